@@ -1,0 +1,367 @@
+"""Benchmark of the well-balanced Euler-with-gravity step (DOF-updates/s).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (N=1): the 8192x8192 P2 bandwidth-stress configuration -- isothermal
+atmosphere Phi = 0.1 y, rho = p = exp(-0.1 y), 16-mode seeded velocity perturbation of
+amplitude 1e-2 -- advanced by SSP-RK2 with device-computed CFL steps (CFL 0.3) in the
+FP32-perturbation form.  One step = one full time step (two fused RK stages + CFL
+reduction) over the whole grid.  Inputs (6.4 GB of FP32 state) are far larger than L2.
+Beside it: the FP64 plain method on the same grid (DOF-updates/s and the L1 error of the
+FP32 form against it), the end-to-end rate through the C ABI with pinned host buffers,
+and the CPU oracle on a bounded sample.  For N > 1 (torchrun) every rank advances its own
+independent replica ("replicas only": the path has no data exchange on one GPU each).
+"""
+import argparse
+import csv
+import importlib.util
+import io
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+METRIC = "DOF-updates/s on 1 GB300: FP32-perturbation vs FP64 plain at L1 err<=1e-6"
+UNIT = "DOF-updates/s"
+BYTES_PER_DOF_UPDATE = {"fp32": 20.0, "fp64": 40.0}  # SSP-RK2: 5 state accesses per DOF
+
+
+def load_package():
+    name = "fvm_source_wb_gb300"
+    if name in sys.modules:
+        return sys.modules[name]
+    spec = importlib.util.spec_from_file_location(
+        name, os.path.join(ROOT, "fvm-source-wb_gb300", "__init__.py"))
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[name] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def measured_hbm_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(workload):
+    """Per-launch DRAM bytes of the stage kernel from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "k_stage_%s_traffic.json" % workload)
+    try:
+        with open(p) as f:
+            return json.load(f)
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.f = tempfile.TemporaryFile(mode="w+")
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.seek(0)
+        rows = [r for r in csv.reader(io.StringIO(self.f.read())) if len(r) >= 9]
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if "Active" in r[5 + k]
+                          and "Not" not in r[5 + k]})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return None, 0, 1, int(os.environ.get("LOCAL_RANK", "0"))
+    import torch
+    import torch.distributed as dist
+    lr = int(os.environ.get("LOCAL_RANK", "0"))
+    backend = "nccl" if torch.cuda.is_available() else "gloo"
+    if backend == "nccl":
+        torch.cuda.set_device(lr)
+    dist.init_process_group(backend=backend)
+    return dist, dist.get_rank(), dist.get_world_size(), lr
+
+
+def reduce_max(dist, x, device):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64,
+                     device="cuda:%d" % device if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+# ---------------------------------------------------------------- CPU baseline
+
+def cpu_sample(wb, seconds=12.0, n=512, min_steps=2, warm=1, threads=None):
+    """The FP64 CPU oracle (OpenMP, all host threads) on an n x n grid with the cfg5
+    physics; returns (DOF-updates/s, threads, sample description)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+    threads = threads or os.cpu_count() or 1
+    O.set_threads(threads)
+    w = wb.workload("cfg5", nx=n, ny=n)
+    oc = O.make_cfg(nx=n, ny=n, order=w["order"], basis=w["basis"], bc_x=w["bc_x"],
+                    bc_y=w["bc_y"], eq_kind=w["eq_kind"], gx=w["gx"], gy=w["gy"],
+                    rho0=w["rho0"], p0=w["p0"], limiter=w["limiter"], cfl=w["cfl"])
+    ic = wb.workload_ic("cfg5")
+    oic = O.make_ic(kind=2, amp=ic.amp, nmodes=ic.nmodes, kx=list(ic.kx), ky=list(ic.ky),
+                    phase_u=list(ic.phase_u), phase_v=list(ic.phase_v), weight=list(ic.weight))
+    d = O.project_ic(oc, oic)
+    dof = d.size
+    if warm:
+        d, _ = O.run_rk2(oc, d, warm, -1.0)
+    steps, t0 = 0, time.perf_counter()
+    while steps < min_steps or time.perf_counter() - t0 < seconds:
+        d, _ = O.run_rk2(oc, d, 1, -1.0)
+        steps += 1
+    el = time.perf_counter() - t0
+    desc = ("FP64 oracle port (C, OpenMP) on %dx%d cells of the cfg5 physics (P2, "
+            "isothermal Phi=0.1y, 16-mode velocity field), %d SSP-RK2 CFL steps, %.1f s"
+            % (n, n, steps, el))
+    return dof * steps / el, threads, desc
+
+
+def run_reference(args):
+    dist, rank, world, lr = dist_init()
+    if rank != 0:
+        return 0
+    wb = load_package()
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    n = args.ref_n
+    w = wb.workload("cfg5", nx=n, ny=n)
+    oc = O.make_cfg(nx=n, ny=n, order=w["order"], basis=w["basis"], bc_x=w["bc_x"],
+                    bc_y=w["bc_y"], eq_kind=w["eq_kind"], gx=w["gx"], gy=w["gy"],
+                    rho0=w["rho0"], p0=w["p0"], limiter=w["limiter"], cfl=w["cfl"])
+    ic = wb.workload_ic("cfg5")
+    oic = O.make_ic(kind=2, amp=ic.amp, nmodes=ic.nmodes, kx=list(ic.kx), ky=list(ic.ky),
+                    phase_u=list(ic.phase_u), phase_v=list(ic.phase_v), weight=list(ic.weight))
+    d = O.project_ic(oc, oic)
+    dof = d.size
+    d, _ = O.run_rk2(oc, d, args.warmup, -1.0)
+    t0 = time.perf_counter()
+    d, _ = O.run_rk2(oc, d, args.steps, -1.0)
+    el = time.perf_counter() - t0
+    value = dof * args.steps / el
+    sample = ("each step: one SSP-RK2 CFL step of the FP64 oracle port (the reference's "
+              "Fortran cannot be compiled here) on %dx%d cells of the cfg5 physics" % (n, n))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": "cfg5: 8192^2 P2 isothermal Phi=0.1y, 16-mode velocity field "
+                               "(CPU sample %dx%d)" % (n, n), "order": 2, "basis": "P",
+                   "dofs_per_step": dof, "l2_policy": "n/a (CPU)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------------------- our arm
+
+def run_ours(args):
+    import torch
+    dist, rank, world, lr = dist_init()
+    wb = load_package()
+    wb.lib()  # raises if the CUDA library is missing: there is no CPU fallback
+    dev = lr
+    torch.cuda.set_device(dev)
+    name = args.workload
+    w32 = wb.workload(name, wb.PREC_FP32)
+    ic = wb.workload_ic(name)
+    s32 = wb.Solver(device=dev, **w32)
+    dof = s32.dofs
+    s32.init_perturbation(ic)
+    s32.step(args.warmup)
+    s32.sync()
+    stream = torch.cuda.ExternalStream(s32.stream(), device=dev)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    sampler = ClockSampler(dev) if rank == 0 else None
+    barrier(dist)
+    torch.cuda.synchronize()
+    if sampler:
+        sampler.start()
+    s32.profile_stages(True)
+    e0.record(stream)
+    s32.step(args.steps)
+    e1.record(stream)
+    e1.synchronize()
+    s32.sync()
+    torch.cuda.synchronize()
+    barrier(dist)
+    clocks = sampler.stop() if sampler else None
+    ms = e0.elapsed_time(e1)
+    stage_ms, launches = s32.stage_stats()
+    s32.profile_stages(False)
+    ms_max = reduce_max(dist, ms, dev)
+    value = world * dof * args.steps / (ms_max / 1e3)
+
+    # roofline of the dominant kernel (the fused stage kernel: every launch in the region)
+    peak, peak_kind = measured_hbm_peak()
+    per_launch_bytes = BYTES_PER_DOF_UPDATE["fp32"] * dof / 2.0
+    avg_launch_s = stage_ms / max(launches, 1) / 1e3
+    achieved = per_launch_bytes / avg_launch_s / 1e9
+    traffic = ncu_traffic(name)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_kind": peak_kind,
+                "traffic": traffic.get("bytes_per_launch") if traffic else None,
+                "kernel": "k_stage<float,2,P>", "algorithmic_bytes_per_launch": per_launch_bytes,
+                "avg_launch_ms": avg_launch_s * 1e3}
+
+    extra = {}
+    if rank == 0 and not args.quick:
+        # FP64 plain on the same grid
+        w64 = wb.workload(name, wb.PREC_FP64)
+        s64 = wb.Solver(device=dev, **w64)
+        s64.init_perturbation(ic)
+        s64.step(1)
+        s64.sync()
+        st64 = torch.cuda.ExternalStream(s64.stream(), device=dev)
+        a0 = torch.cuda.Event(enable_timing=True)
+        a1 = torch.cuda.Event(enable_timing=True)
+        a0.record(st64)
+        s64.step(args.plain_steps)
+        a1.record(st64)
+        a1.synchronize()
+        s64.sync()
+        v64 = dof * args.plain_steps / (a0.elapsed_time(a1) / 1e3)
+        # L1 of the FP32 form against the FP64 plain method, same fixed steps
+        s64.init_perturbation(ic)
+        s32b = wb.Solver(device=dev, **w32)
+        s32b.init_perturbation(ic)
+        sx, sy = s64.compute_max_speed()
+        dx = 1.0 / w64["nx"]
+        dt = w64["cfl"] / (2 * w64["order"] + 1) / (sx / dx + sy / dx)
+        s64.step(args.check_steps, dt)
+        s32b.step(args.check_steps, dt)
+        l1, linf, _ = s32b.compute_error(s64)
+        ref1, _, _ = s64.compute_error(None)
+        s32b.close()
+        s64.close()
+        extra["fp64_plain"] = {"value": v64, "unit": UNIT, "steps": args.plain_steps,
+                               "speedup_fp32_over_fp64": value / world / v64}
+        extra["accuracy"] = {"l1_fp32_vs_fp64": l1.tolist(), "linf_fp32_vs_fp64": linf.tolist(),
+                             "l1_perturbation_fp64": ref1.tolist(), "steps": args.check_steps,
+                             "dt": dt, "l1_bar": 1e-6, "pass": bool(np.all(l1 <= 1e-6))}
+
+    # end to end through the C ABI: pinned host state in, one step, state out
+    e2e = None
+    if not args.no_e2e:
+        host_in = torch.empty(dof, dtype=torch.float32, pin_memory=True)
+        host_out = torch.empty(dof, dtype=torch.float32, pin_memory=True)
+        s32.download_f32_ptr(host_out.data_ptr())
+        host_in.copy_(host_out)
+        nE = args.e2e_steps
+        barrier(dist)
+        t0 = time.perf_counter()
+        for _ in range(nE):
+            s32.upload_f32_ptr(host_in.data_ptr())
+            s32.step(1)
+            s32.download_f32_ptr(host_out.data_ptr())
+        el = reduce_max(dist, time.perf_counter() - t0, dev)
+        e2e = {"value": world * dof * nE / el, "unit": UNIT, "h2d_bytes_per_step": dof * 4,
+               "d2h_bytes_per_step": dof * 4, "steps": nE,
+               "path": "wb_upload_state_f32 + wb_step + wb_download_state_f32, pinned host"}
+    s32.close()
+
+    cpu = None
+    if rank == 0 and not args.quick:
+        v, cores, desc = cpu_sample(wb, seconds=args.cpu_seconds)
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded 16-mode velocity field on the isothermal atmosphere)",
+            "config": {"workload": "cfg5: 8192^2 P2 isothermal Phi=0.1y, 16-mode velocity field, "
+                                   "FP32-perturbation, SSP-RK2, CFL 0.3",
+                       "nx": w32["nx"], "ny": w32["ny"], "order": 2, "basis": "P",
+                       "dofs": dof, "parallelism": "replicas" if world > 1 else "single",
+                       "l2_policy": "inputs larger than L2 (6.4 GB state per buffer)"},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+            "clocks": clocks,
+        }
+        line.update(extra)
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="cfg5")
+    ap.add_argument("--plain-steps", type=int, default=2)
+    ap.add_argument("--check-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--ref-n", type=int, default=512)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--quick", action="store_true", help="skip FP64, accuracy and CPU legs")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

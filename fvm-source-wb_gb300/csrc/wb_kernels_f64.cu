@@ -1,0 +1,34 @@
+// wb_kernels_f64.cu -- FP64 "plain" instantiations and the FP64 diagnostics.
+#include "wb_types.h"
+namespace wb {
+__constant__ Tab1D<double> c_tab[KMAX + 1];
+}
+#include "wb_launch.cuh"
+WB_DEFINE_PRECISION_ENTRY_POINTS(double)
+
+namespace wb {
+
+size_t diag_partial_bytes(int nx, int ny) {
+  size_t nblk = (size_t)((nx + 31) / 32) * ((ny + 7) / 8);
+  return nblk * NV * 3 * sizeof(double) + 64 * sizeof(double);
+}
+
+cudaError_t launch_norms(const AuxArgs &A, const Tab1D<double> *Td, const double *a,
+                         const double *b, double *partial, double *out, int K_, int B_,
+                         cudaStream_t s) {
+  dim3 blk(32, 8), grd = cell_grid(A.nx, A.ny, blk);
+  WB_DISPATCH_KB(K_, B_, { k_norms<K, BASIS><<<grd, blk, 0, s>>>(A, Td, a, b, partial); });
+  k_norms_final<<<1, 32, 0, s>>>(partial, (int)(grd.x * grd.y), out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_f32_to_f64(double *out, const float *in, long long n, cudaStream_t s) {
+  k_convert<double, float><<<1216, 256, 0, s>>>(out, in, n);
+  return cudaGetLastError();
+}
+cudaError_t launch_f64_to_f32(float *out, const double *in, long long n, cudaStream_t s) {
+  k_convert<float, double><<<1216, 256, 0, s>>>(out, in, n);
+  return cudaGetLastError();
+}
+
+}  // namespace wb

@@ -1,0 +1,120 @@
+// wb_types.h -- types shared by the host layer and the sm_103a kernels.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace wb {
+
+constexpr int NV = 4;      // conserved variables (rho, mx, my, E)
+constexpr int KMAX = 2;    // highest polynomial degree compiled
+constexpr int NQMAX = KMAX + 1;
+
+// Modes per variable for degree k and basis (0 = tensor Q_k, 1 = total degree P_k).
+__host__ __device__ constexpr int num_modes(int k, int basis) {
+  return basis == 0 ? (k + 1) * (k + 1) : (k + 1) * (k + 2) / 2;
+}
+// Mode m -> (a, b) in graded order (total degree, then a descending).
+__host__ __device__ constexpr int mode_deg(int k, int basis, int m, int which) {
+  int n = 0;
+  int dmax = basis == 0 ? 2 * k : k;
+  for (int d = 0; d <= dmax; ++d)
+    for (int a = d; a >= 0; --a) {
+      int b = d - a;
+      if (a <= k && b <= k) {
+        if (n == m) return which == 0 ? a : b;
+        ++n;
+      }
+    }
+  return -1;
+}
+__host__ __device__ constexpr int mode_index(int k, int basis, int a, int b) {
+  int n = 0;
+  int dmax = basis == 0 ? 2 * k : k;
+  for (int d = 0; d <= dmax; ++d)
+    for (int aa = d; aa >= 0; --aa) {
+      int bb = d - aa;
+      if (aa <= k && bb <= k) {
+        if (aa == a && bb == b) return n;
+        ++n;
+      }
+    }
+  return -1;
+}
+
+// One-dimensional Gauss-Legendre tables for nq = k+1 points, basis
+// phi_a = sqrt(2a+1) P_a.  B = phi_a(xi_q), D = phi_a'(xi_q), BW = B*w, DW = D*w,
+// Ep/Em = phi_a(+1)/phi_a(-1).
+template <typename R>
+struct Tab1D {
+  R xq[NQMAX], wq[NQMAX];
+  R B[NQMAX][NQMAX], D[NQMAX][NQMAX], BW[NQMAX][NQMAX], DW[NQMAX][NQMAX];
+  R Ep[NQMAX], Em[NQMAX];
+};
+
+// Device-resident run state: simulated time, step count, the fused wave-speed maxima
+// (non-negative doubles stored as their bit patterns so atomicMax orders them) and
+// the non-physical-state flag.  Double-buffered by step parity.
+struct DevState {
+  double t[2];
+  unsigned long long smax[2][2];  // [parity][direction]
+  long long nstep[2];
+  int err;
+  int pad;
+};
+
+// One output of a stage: out = sum_i c_i * [lim](in_i) + beta * Y + cdt * dt * L(Y).
+template <typename R>
+struct Combo {
+  R *out;
+  const R *in[2];
+  R c[2];
+  int lim[2];
+  R beta, cdt;
+};
+
+template <typename R>
+struct StageArgs {
+  const R *x;                 // stage input (loaded with halo, limited if lim_y)
+  Combo<R> o[2];              // o[1].out may be null
+  int nx, ny;
+  long long plane;            // elements between (var, mode) planes
+  int bc_x, bc_y, llf_speed, limiter, lim_y;
+  int eq_kind;
+  R dx, dy, hidx, hidy;       // hidx = 0.5/dx, hidy = 0.5/dy
+  R gamma, gm1, igm1, hgam;   // hgam = gamma/(gamma-1)
+  R gx, gy;
+  R rho0, p0, kpoly, npoly;   // npoly = 1/(gamma-1)
+  R lim_norm, lim_Mdx2, lim_Mdy2, lim_tol;
+  // separable equilibrium factors: x at volume points [nx*nq], x at faces [nx+1], y likewise
+  const R *fxv, *fxf, *fyv, *fyf;
+  // time step
+  int dt_mode;                // 0 fixed dt_fixed, 1 CFL from dev->smax[parity]
+  int parity;
+  int advance_time;           // first stage of a step: t[parity^1] = t[parity] + dt
+  int compute_speed;          // last stage of a step: accumulate smax[parity^1]
+  double dt_fixed;
+  double cfl_over;            // cfl / (2k+1)
+  double tend;                // > 0: clip dt at tend - t
+  double ddx, ddy;            // dx, dy in double
+  DevState *dev;
+};
+
+// Arguments of the per-cell auxiliary kernels (FP64 equilibrium factors).
+struct AuxArgs {
+  int nx, ny;
+  long long plane;
+  int bc_x, bc_y, limiter, eq_kind;
+  double dx, dy, gamma, gx, gy, rho0, p0, kpoly, npoly;
+  double lim_norm, lim_Mdx2, lim_Mdy2, lim_tol;
+  const double *fxv, *fxf, *fyv, *fyf;  // FP64 separable equilibrium factors
+};
+
+// Seeded perturbation (initial condition) parameters.
+struct IcArgs {
+  int kind, nmodes;
+  double amp, xc, yc, sigma;
+  double kx[32], ky[32], pu[32], pv[32], wt[32];
+};
+
+}  // namespace wb

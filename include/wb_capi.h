@@ -1,0 +1,199 @@
+/*
+ * wb_capi.h -- C ABI of the GB300-native well-balanced Euler-with-gravity step.
+ *
+ * Drop-in boundary for the step routines of hanveiga/fvm-source-wb.  The reference
+ * binds them as Fortran external subroutines with implicit interfaces and sizes taken
+ * from module parameters; a Fortran driver reaches this library through an
+ * ISO_C_BINDING interface module (bind(C, name="wb_...")), see INTEGRATION.md.
+ *
+ * Conventions
+ *   - every entry point returns an int status: WB_OK (0) or a negative WB_ERR_* code;
+ *     wb_last_error(ctx) gives the message of the last failure on that context;
+ *   - host arrays are caller-owned and only read/written during the call;
+ *   - device buffers are owned by the context; one CUDA stream per context; a context
+ *     is used by one host thread at a time;
+ *   - modal state layout WB_LAYOUT_SOA:        delta[(v*nb + m)*ny*nx + j*nx + i]
+ *                  layout WB_LAYOUT_FORTRAN:    u(nvar, nx, ny, k+1, k+1) column-major,
+ *                  the reference's array layout (tensor basis WB_BASIS_Q only);
+ *     v = 0..3 is (rho, rho*u, rho*v, E) of the PERTURBATION about the equilibrium;
+ *     mode m <-> degrees (a, b) as listed by wb_mode_list.
+ */
+#ifndef WB_CAPI_H
+#define WB_CAPI_H
+#include <stddef.h>
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define WB_OK 0
+#define WB_ERR_CONFIG (-1)      /* invalid configuration */
+#define WB_ERR_CUDA (-2)        /* CUDA runtime failure (message keeps cudaGetErrorString) */
+#define WB_ERR_NONPHYSICAL (-3) /* device flag: non-finite or non-positive rho/p in a cell mean */
+#define WB_ERR_TIMEOUT (-4)     /* a bounded device wait gave up */
+#define WB_ERR_ARG (-5)         /* bad argument (null pointer, bad layout, size out of range) */
+#define WB_ERR_NOMEM (-6)       /* device allocation failed */
+#define WB_ERR_STATE (-7)       /* call not valid in the context's current state */
+
+/* enumerations */
+#define WB_BASIS_Q 0        /* tensor Legendre Q_k, (k+1)^2 modes (2d/benchmark_2d_dg.f90) */
+#define WB_BASIS_P 1        /* total-degree P_k, (k+1)(k+2)/2 modes */
+#define WB_BC_PERIODIC 0    /* bc=1 of 2d/parameters_dg_2d.f90 */
+#define WB_BC_COPY 1        /* bc=2,3: ghost = copy of the edge cell's perturbation */
+#define WB_EQ_NONE 0        /* zero equilibrium (nequilibrium=3) */
+#define WB_EQ_ISOTHERMAL 1  /* rho = rho0 exp(-(rho0/p0) Phi), p = p0 exp(-(rho0/p0) Phi) */
+#define WB_EQ_POLYTROPE 2   /* p = K rho^gamma, rho = (1 - (gamma-1)/(gamma K) Phi)^(1/(gamma-1)) */
+#define WB_LLF_MAXABS 0     /* lambda = max(|v_n|+c) over both sides */
+#define WB_LLF_REF2D 1      /* lambda = max(|v_n+c|) as compute_llflux of 2d/benchmark_2d_dg.f90 */
+#define WB_PREC_FP64 0      /* "plain": FP64 state, literal F(u_eq+d) - F(u_eq) split */
+#define WB_PREC_FP32 1      /* FP64 equilibrium tables + FP32 perturbation, exact-difference fluxes */
+#define WB_RK2 0            /* SSP-RK2 ('EQL' branch of evolve) */
+#define WB_RK54 1           /* SSP-RK(5,4) ('RK4' branch of evolve) */
+#define WB_LAYOUT_SOA 0
+#define WB_LAYOUT_FORTRAN 1
+
+typedef struct {
+  int32_t nx, ny;        /* cells per direction (>= 1) */
+  int32_t order;         /* polynomial degree k, 0..2 */
+  int32_t basis;         /* WB_BASIS_* */
+  int32_t bc_x, bc_y;    /* WB_BC_* */
+  int32_t eq_kind;       /* WB_EQ_* */
+  int32_t llf_speed;     /* WB_LLF_* */
+  int32_t limiter;       /* 0 off, 1 minmod moment limiter on the perturbation */
+  int32_t precision;     /* WB_PREC_* */
+  int32_t integrator;    /* WB_RK2 or WB_RK54 */
+  int32_t tile_x, tile_y;/* CTA tile in cells; 0 = tuned default */
+  int32_t device;        /* CUDA device ordinal */
+  double gamma;
+  double gx, gy;         /* Phi = gx x + gy y */
+  double rho0, p0;       /* isothermal reference state */
+  double kpoly;          /* polytropic constant K */
+  double lx, ly;         /* domain [0,lx] x [0,ly] */
+  double lim_norm;       /* minmod slope scaling (reference: 3) */
+  double lim_M;          /* TVB constant M (slopes with |norm s| < M h^2 untouched) */
+  double lim_tol;        /* re-limit a cell only if a slope changes by more than this */
+  double cfl;            /* CFL number */
+} wb_config;
+
+/* seeded perturbation generator (initial condition), evaluated on the device in FP64 */
+typedef struct {
+  int32_t kind;          /* 0 zero, 1 Gaussian pressure bump, 2 multimode velocity */
+  int32_t nmodes;        /* kind 2: Fourier modes (<= 32) */
+  double amp;
+  double xc, yc, sigma;  /* kind 1 */
+  double kx[32], ky[32], phase_u[32], phase_v[32], weight[32]; /* kind 2 */
+} wb_perturbation;
+
+typedef struct wb_ctx wb_ctx;
+
+/* --- configuration and lifetime ------------------------------------------------ */
+/* Fills the reference's defaults (2d/parameters_dg_2d.f90:1-40 where they apply). */
+int wb_config_default(wb_config *cfg);
+/* Creates a context: validates cfg, allocates the state and equilibrium tables on
+ * cfg->device.  Replaces the module-parameter setup of 2d/parameters_dg_2d.f90 and
+ * get_coords/get_equilibrium_solution (2d/benchmark_2d_dg.f90:93-120,594-622). */
+int wb_create(const wb_config *cfg, wb_ctx **out);
+int wb_destroy(wb_ctx *ctx);
+const char *wb_last_error(const wb_ctx *ctx);
+const char *wb_status_string(int status);
+/* number of modes per variable; the (a,b) degree list in the library's order */
+int wb_num_modes(int order, int basis);
+int wb_mode_list(int order, int basis, int32_t *deg_x, int32_t *deg_y);
+
+/* --- state transfer ------------------------------------------------------------ */
+/* Upload / download the perturbation modes (FP64 host arrays).  Download returns the
+ * limited state, i.e. what apply_limiter would leave after the last stage. */
+int wb_upload_state(wb_ctx *ctx, const double *delta, int32_t layout);
+int wb_download_state(wb_ctx *ctx, double *delta, int32_t layout);
+/* same with FP32 host arrays (SoA only) */
+int wb_upload_state_f32(wb_ctx *ctx, const float *delta);
+int wb_download_state_f32(wb_ctx *ctx, float *delta);
+/* Projects a seeded perturbation onto the modes on the device (the IC + projection of
+ * get_initial_conditions/get_modes_from_nodes, 2d/benchmark_2d_dg.f90:122-153,497-542);
+ * resets t and the step counter. */
+int wb_init_perturbation(wb_ctx *ctx, const wb_perturbation *ic);
+/* Device address of the resident state (SoA, element type per precision) and the
+ * element stride between (variable, mode) planes. */
+int wb_device_state(wb_ctx *ctx, void **dptr, size_t *plane_stride);
+
+/* --- the step routines ------------------------------------------------------- */
+/* dudt = L(delta) for host arrays: drop-in for compute_update(delta_u, x, y, u_eq, dudt),
+ * 2d/benchmark_2d_dg.f90:1137-1479 (x, y, u_eq are implied by the context), in the
+ * well-balanced split of compute_update_exact_delta, dg_with_source.f90:1749-2031.
+ * The input is not limited (compute_update does not limit). */
+int wb_compute_update(wb_ctx *ctx, const double *delta_u, double *dudt, int32_t layout);
+/* Limits the resident state in place: apply_limiter(u), 2d/benchmark_2d_dg.f90:1516-1555
+ * with compute_limiter, 2d/limiters.f90:203-309, applied to the perturbation. */
+int wb_apply_limiter(wb_ctx *ctx);
+/* Directional maximum wave speeds max(|u|+c), max(|v|+c) over cell means of the full
+ * state: compute_max_speed(u, cs_max, v_xmax, v_ymax, speed_max), :826-870. */
+int wb_max_speed(wb_ctx *ctx, double *smax_x, double *smax_y);
+/* Advances nsteps time steps with cfg->integrator (the stage loop of evolve,
+ * 2d/benchmark_2d_dg.f90:666-747).  dt > 0: fixed step; dt <= 0: CFL step computed
+ * on the device every step from the fused wave-speed reduction.  Asynchronous on the
+ * context stream; errors from the device flag surface at the next synchronising call. */
+int wb_step(wb_ctx *ctx, int32_t nsteps, double dt);
+/* Runs until t >= tend (or max_steps) with CFL steps clipped at tend: evolve,
+ * 2d/benchmark_2d_dg.f90:624-775.  Synchronising. */
+int wb_evolve(wb_ctx *ctx, double tend, int32_t max_steps, int32_t *steps_done, double *t_out);
+/* Waits for the context stream; reports a device-side non-physical flag. */
+int wb_sync(wb_ctx *ctx);
+int wb_get_time(wb_ctx *ctx, double *t, int64_t *steps);
+
+/* The context's CUDA stream (a cudaStream_t), for callers that order their own work
+ * against it or time it with CUDA events.  No counterpart in the reference (serial). */
+int wb_get_stream(wb_ctx *ctx, void **stream);
+/* When on, every stage-kernel launch is bracketed by CUDA events on the context stream;
+ * wb_stage_stats returns the summed kernel time and launch count since the last call
+ * (and resets them).  No counterpart in the reference (it has no timers). */
+int wb_profile_stages(wb_ctx *ctx, int32_t on);
+int wb_stage_stats(wb_ctx *ctx, double *total_ms, int64_t *launches);
+
+/* --- diagnostics ---------------------------------------------------------------- */
+/* Error norms of the (limited) resident state against another context's state on the
+ * same grid and basis (other may be NULL: norms of the state itself), in FP64:
+ * compute_error, 2d/benchmark_2d_dg.f90:23-89 (L1, Linf, L2 per conserved variable). */
+int wb_norms(wb_ctx *ctx, wb_ctx *other, double l1[4], double linf[4], double l2[4]);
+/* FP64 domain integrals of the full conserved state (equilibrium + perturbation). */
+int wb_conserved_sums(wb_ctx *ctx, double sums[4]);
+
+/* --- batched form -------------------------------------------------------------- */
+typedef struct wb_batch wb_batch;
+/* n independent instances (each its own grid, order, basis, equilibrium, limiter),
+ * FP32-perturbation form, advanced together: one persistent launch per RK stage over
+ * a work list of cell tiles.  All cfgs must share precision, integrator and device. */
+int wb_batch_create(const wb_config *cfgs, int32_t n, wb_batch **out);
+int wb_batch_destroy(wb_batch *b);
+const char *wb_batch_last_error(const wb_batch *b);
+int wb_batch_init_perturbation(wb_batch *b, const wb_perturbation *ics);
+/* nsteps steps; each instance takes its own CFL dt (dt <= 0) or the fixed dt */
+int wb_batch_step(wb_batch *b, int32_t nsteps, double dt);
+int wb_batch_sync(wb_batch *b);
+int wb_batch_download(wb_batch *b, int32_t index, double *delta);
+int wb_batch_total_dofs(wb_batch *b, int64_t *dofs);
+
+/* --- 1D well-balanced finite volume (the fvm.f90 / benchmark_1d.f90 path) --------- */
+typedef struct wb1d_ctx wb1d_ctx;
+typedef struct {
+  int32_t nx;
+  int32_t bc;            /* WB_BC_PERIODIC or WB_BC_COPY (equilibrium-extrapolated) */
+  int32_t limiter;       /* 0 first order, 1 minmod MUSCL on the perturbation */
+  int32_t eq_kind;       /* WB_EQ_ISOTHERMAL or WB_EQ_POLYTROPE */
+  int32_t device;
+  int32_t pad;
+  double gamma, g, rho0, p0, kpoly, lx, cfl;
+} wb1d_config;
+/* compute_update 'EQL' + evolve of benchmark_1d.f90:200-377 on the device */
+int wb1d_create(const wb1d_config *cfg, wb1d_ctx **out);
+int wb1d_destroy(wb1d_ctx *c);
+const char *wb1d_last_error(const wb1d_ctx *c);
+int wb1d_upload(wb1d_ctx *c, const double *delta);      /* delta[i*3 + v] */
+int wb1d_download(wb1d_ctx *c, double *delta);
+int wb1d_compute_update(wb1d_ctx *c, const double *delta, double *dudt);
+int wb1d_evolve(wb1d_ctx *c, double tend, int32_t max_steps, int32_t *steps_done, double *t_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,40 @@
+"""Shared fixtures.  GPU tests are marked `gpu`; everything else runs on CPU."""
+import ctypes
+import importlib.util
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (runs through the C ABI)")
+
+
+def load_package():
+    name = "fvm_source_wb_gb300"
+    if name in sys.modules:
+        return sys.modules[name]
+    spec = importlib.util.spec_from_file_location(
+        name, os.path.join(ROOT, "fvm-source-wb_gb300", "__init__.py"))
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[name] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+@pytest.fixture(scope="session")
+def wb():
+    return load_package()
+
+
+@pytest.fixture(scope="session")
+def orc():
+    import pyoracle
+    pyoracle.lib()
+    return pyoracle

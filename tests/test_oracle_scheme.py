@@ -1,0 +1,129 @@
+"""Properties of the oracle's scheme (CPU): exact well-balance, agreement with the
+literal restatements of the reference operators, conservation, limiter behaviour and
+the 1D finite-volume path."""
+import numpy as np
+import pytest
+
+from helpers import base_cfg, orc_cfg, random_delta
+
+
+@pytest.mark.parametrize("order,basis", [(0, 0), (1, 0), (1, 1), (2, 0), (2, 1)])
+@pytest.mark.parametrize("eq_kind", [1, 2])
+def test_zero_perturbation_exact(orc, order, basis, eq_kind):
+    c = base_cfg(order=order, basis=basis, eq_kind=eq_kind, gx=0.4, gy=1.0, limiter=1)
+    oc = orc_cfg(c)
+    z = np.zeros((4, orc.nb(oc), c["ny"], c["nx"]))
+    assert np.all(orc.rhs(oc, z) == 0.0)
+    d, _ = orc.run_rk2(oc, z, 50, -1.0)
+    assert np.all(d == 0.0)
+
+
+@pytest.mark.parametrize("order", [0, 1, 2])
+@pytest.mark.parametrize("bc", [1, 2])
+def test_matches_literal_reference_2d_operator(orc, order, bc):
+    """Zero equilibrium, no gravity: the composed operator is the reference's
+    2d/benchmark_2d_dg.f90 compute_update (with its 'llf1' flux branch taken)."""
+    nx = ny = 6
+    m = order + 1
+    c = base_cfg(nx=nx, ny=ny, order=order, basis=0, eq_kind=0, gx=0.0, gy=0.0,
+                 bc_x=0 if bc == 1 else 1, bc_y=0 if bc == 1 else 1, llf_speed=1)
+    oc = orc_cfg(c)
+    rng = np.random.default_rng(order)
+    d = random_delta(c, amp=1e-1, seed=order)
+    d[0, 0] += 1.0
+    d[3, 0] += 2.5
+    a, b = orc.modes(order, 0)
+    f = np.zeros((4, nx, ny, m, m), order="F")
+    for k in range(len(a)):
+        f[:, :, :, a[k], b[k]] = d[:, k].transpose(0, 2, 1)
+    ref = orc.ref2d_compute_update(f, nx, ny, m, bc=bc)
+    got = orc.rhs(oc, d)
+    for k in range(len(a)):
+        np.testing.assert_allclose(got[:, k].transpose(0, 2, 1), ref[:, :, :, a[k], b[k]],
+                                   rtol=0, atol=1e-13)
+
+
+def test_reference_flux_type_defect_reproduced(orc):
+    """flux_type='llf' never matches 'llf1' (2d/benchmark_2d_dg.f90:999): faces stay zero."""
+    nx = ny = 4
+    u = np.zeros((4, nx, ny, 2, 2), order="F")
+    u[0] = 1.0
+    u[3] = 2.5
+    u[1, :, :, 1, 0] = 0.1
+    r_bug = orc.ref2d_compute_update(u, nx, ny, 2, flux_bug=1)
+    r_ok = orc.ref2d_compute_update(u, nx, ny, 2, flux_bug=0)
+    assert not np.allclose(r_bug, r_ok)
+
+
+@pytest.mark.parametrize("order", [0, 1, 2])
+def test_matches_literal_reference_1d_wb_operator(orc, order):
+    """y-uniform data reduce the 2D well-balanced operator to the 1D
+    compute_update_exact_delta of dg_with_source.f90:1749-2031 (interior cells)."""
+    n, nx = order + 1, 10
+    c = base_cfg(nx=nx, ny=1, order=order, basis=0, eq_kind=1, gx=1.0, gy=0.0, bc_x=0, bc_y=0)
+    oc = orc_cfg(c)
+    a, b = orc.modes(order, 0)
+    rng = np.random.default_rng(1)
+    d = np.zeros((4, len(a), 1, nx))
+    d1 = np.zeros((3, n, nx), order="F")
+    for k in range(n):
+        mm = [i for i in range(len(a)) if a[i] == k and b[i] == 0][0]
+        vals = 1e-2 * rng.standard_normal((3, nx))
+        d[0, mm, 0], d[1, mm, 0], d[3, mm, 0] = vals
+        d1[:, k, :] = vals
+    r2 = orc.rhs(oc, d)
+    r1 = orc.dg1d_update_exact_delta(d1, nx, n)
+    for k in range(n):
+        mm = [i for i in range(len(a)) if a[i] == k and b[i] == 0][0]
+        for v2, v1 in ((0, 0), (1, 1), (3, 2)):
+            np.testing.assert_allclose(r2[v2, mm, 0, 1:-1], r1[v1, k, 1:-1], rtol=0, atol=5e-14)
+        assert np.max(np.abs(r2[2])) < 1e-16
+
+
+def test_conservation_periodic(orc):
+    c = base_cfg(nx=10, ny=8, order=2, basis=1, bc_x=0, bc_y=0, eq_kind=1, gx=0.0, gy=0.0)
+    oc = orc_cfg(c)
+    d = random_delta(c, seed=4)
+    r = orc.rhs(oc, d)
+    # mode 0 carries the cell mean: its domain sum changes only by boundary fluxes (none)
+    assert np.all(np.abs(r[:, 0].sum(axis=(1, 2))) < 1e-13)
+
+
+def test_limiter_idempotent_and_selective(orc):
+    c = base_cfg(nx=16, ny=16, order=2, basis=1, limiter=1)
+    oc = orc_cfg(c)
+    d = random_delta(c, amp=1e-1, seed=8, smooth=False)
+    l1 = orc.limit(oc, d)
+    assert np.array_equal(orc.limit(oc, l1), l1)
+    assert np.array_equal(l1[:, 0], d[:, 0])  # means untouched
+    # a linear perturbation is not limited
+    x = (np.arange(16) + 0.5) / 16
+    lin = np.zeros_like(d)
+    lin[0, 0] = 1e-3 * x[None, :]
+    lin[0, 1] = 1e-3 / 16 / 2 / np.sqrt(3)  # exact slope mode of the linear function
+    np.testing.assert_array_equal(orc.limit(oc, lin)[:, :, :, 1:-1], lin[:, :, :, 1:-1])
+
+
+def test_rk54_consistent_with_rk2(orc):
+    c = base_cfg(nx=16, ny=16, order=1, basis=1, eq_kind=1, bc_x=0, bc_y=1)
+    oc = orc_cfg(c)
+    d = random_delta(c, amp=1e-3, seed=6)
+    a, _ = orc.run_rk2(oc, d, 40, 5e-4)
+    b, _ = orc.run_rk54(oc, d, 20, 1e-3)
+    l1, _, _ = orc.norms(oc, a, b)
+    ref, _, _ = orc.norms(oc, d, np.zeros_like(d))
+    assert np.all(l1[[0, 1, 3]] < 1e-3 * ref[[0, 1, 3]])
+
+
+def test_fv1d_equilibrium_and_perturbation(orc):
+    """Config 1: 1D well-balanced FV (benchmark_1d.f90 'EQL') with minmod MUSCL."""
+    c = orc.make_fv1d(nx=256, bc=1, limiter=1, cfl=0.4)
+    z = np.zeros((256, 3))
+    assert np.all(orc.fv1d_rhs(c, z) == 0.0)
+    zz, t, n = orc.fv1d_run(c, z, 0.25)
+    assert t == pytest.approx(0.25, abs=1e-15) and np.all(zz == 0.0)
+    d0 = orc.fv1d_ic(c)
+    d, t, n = orc.fv1d_run(c, d0, 0.25)
+    assert n > 50
+    # the pressure pulse splits and travels; its energy perturbation stays O(amp)
+    assert 1e-5 < np.max(np.abs(d[:, 2])) < 3e-3
