@@ -8,6 +8,7 @@ configuration; every call goes through libwbgb300.so (CUDA, sm_103a).  There is 
 fallback: if the library is missing or no GPU is present the calls raise.
 """
 import ctypes
+import json
 import math
 import os
 
@@ -77,9 +78,19 @@ def lib():
             "wb_compute_update": ([p, p, p, i32], i32), "wb_apply_limiter": ([p], i32),
             "wb_max_speed": ([p, p, p], i32), "wb_step": ([p, i32, d], i32),
             "wb_evolve": ([p, d, i32, p, p], i32), "wb_sync": ([p], i32),
-            "wb_get_time": ([p, p, p], i32), "wb_norms": ([p, p, p, p, p], i32),
+            "wb_get_time": ([p, p, p], i32), "wb_set_time": ([p, d, ctypes.c_int64], i32),
+            "wb_norms": ([p, p, p, p, p], i32), "wb_write_dat": ([p, ctypes.c_char_p, i32], i32),
             "wb_conserved_sums": ([p, p], i32), "wb_get_stream": ([p, p], i32),
             "wb_profile_stages": ([p, i32], i32), "wb_stage_stats": ([p, p, p], i32),
+            "wb_batch_create": ([p, i32, p], i32), "wb_batch_destroy": ([p], i32),
+            "wb_batch_last_error": ([p], ctypes.c_char_p),
+            "wb_batch_init_perturbation": ([p, p], i32), "wb_batch_step": ([p, i32, d], i32),
+            "wb_batch_sync": ([p], i32), "wb_batch_download": ([p, i32, p], i32),
+            "wb_batch_total_dofs": ([p, p], i32),
+            "wb1d_create": ([p, p], i32), "wb1d_destroy": ([p], i32),
+            "wb1d_last_error": ([p], ctypes.c_char_p), "wb1d_upload": ([p, p], i32),
+            "wb1d_download": ([p, p], i32), "wb1d_compute_update": ([p, p, p], i32),
+            "wb1d_evolve": ([p, d, i32, p, p], i32),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -326,6 +337,61 @@ class Solver:
         self._check(lib().wb_get_time(self._ctx, ctypes.byref(t), ctypes.byref(n)))
         return t.value, n.value
 
+    def output_file(self, path, var=1):
+        """Text snapshot in the reference's output_file format ('(7(1PE12.5,1X))')."""
+        self._check(lib().wb_write_dat(self._ctx, os.fsencode(path), int(var)))
+
+    def set_time(self, t, steps):
+        self._check(lib().wb_set_time(self._ctx, float(t), int(steps)))
+
+    # -- checkpoint / restart (binary: magic, JSON header, raw SoA state)
+    _MAGIC = b"WBGB300\x00"
+
+    def save_checkpoint(self, path):
+        """Writes config, t, step count and the (limited) state; a restart from it
+        continues bitwise identically (the limiter is idempotent on its own output)."""
+        t, n = self.time()
+        state = self.download_f32() if self.dtype == np.float32 else self.download()
+        hdr = {"config": {k: getattr(self.cfg, k) for k, _ in WbConfig._fields_},
+               "t": t, "steps": n, "dtype": str(state.dtype), "shape": list(state.shape)}
+        h = json.dumps(hdr).encode()
+        with open(path, "wb") as f:
+            f.write(self._MAGIC)
+            f.write(np.uint32(len(h)).tobytes())
+            f.write(h)
+            f.write(np.ascontiguousarray(state).tobytes())
+
+    @classmethod
+    def read_checkpoint(cls, path):
+        with open(path, "rb") as f:
+            if f.read(8) != cls._MAGIC:
+                raise ValueError("not a checkpoint: %s" % path)
+            n = int(np.frombuffer(f.read(4), np.uint32)[0])
+            hdr = json.loads(f.read(n).decode())
+            state = np.frombuffer(f.read(), dtype=hdr["dtype"]).reshape(hdr["shape"])
+        return hdr, state
+
+    def load_checkpoint(self, path):
+        hdr, state = self.read_checkpoint(path)
+        c = hdr["config"]
+        for k in ("nx", "ny", "order", "basis", "precision"):
+            if c[k] != getattr(self.cfg, k):
+                raise ValueError("checkpoint %s=%s does not match the solver's %s"
+                                 % (k, c[k], getattr(self.cfg, k)))
+        if state.dtype == np.float32:
+            self.upload_f32(state)
+        else:
+            self.upload(state)
+        self.set_time(hdr["t"], hdr["steps"])
+
+    @classmethod
+    def from_checkpoint(cls, path, device=0):
+        hdr, _ = cls.read_checkpoint(path)
+        c = default_config(**dict(hdr["config"], device=device))
+        s = cls(config=c)
+        s.load_checkpoint(path)
+        return s
+
     def evolve(self, tend, max_steps=2**31 - 1):
         steps = ctypes.c_int32()
         t = ctypes.c_double()
@@ -367,3 +433,157 @@ class Solver:
         s = np.zeros(4)
         self._check(lib().wb_conserved_sums(self._ctx, _ptr(s)))
         return s
+
+
+# ---------------------------------------------------------------- batched form
+
+def batch_workload(n=512, seed_base=1000, nmin=32, nmax=512, device=0):
+    """Independent instances of the batched workload: instance i draws from
+    splitmix64(seed_base + i) its side N = round(exp(U(ln nmin, ln nmax))), degree in
+    {0,1,2}, isothermal or polytropic atmosphere (Phi = y), and a Gaussian pressure bump
+    of amplitude 10^U(-6,-2), centre U(0.2,0.8)^2, width U(0.02,0.1)."""
+    cfgs, ics = [], []
+    for i in range(n):
+        r = SplitMix64(seed_base + i)
+        side = int(round(math.exp(math.log(nmin) + (math.log(nmax) - math.log(nmin)) * r.uniform())))
+        order = min(2, int(3 * r.uniform()))
+        eq = EQ_ISOTHERMAL if r.uniform() < 0.5 else EQ_POLYTROPE
+        amp = 10.0 ** (-6.0 + 4.0 * r.uniform())
+        xc = 0.2 + 0.6 * r.uniform()
+        yc = 0.2 + 0.6 * r.uniform()
+        sigma = 0.02 + 0.08 * r.uniform()
+        c = default_config(nx=side, ny=side, order=order, basis=BASIS_P, bc_x=BC_COPY,
+                           bc_y=BC_COPY, eq_kind=eq, gx=0.0, gy=1.0, rho0=1.0, p0=1.0,
+                           kpoly=1.0, limiter=0, precision=PREC_FP32, integrator=RK2, cfl=0.3,
+                           device=device)
+        cfgs.append(c)
+        ics.append(gaussian_bump(amp, xc, yc, sigma))
+    return cfgs, ics
+
+
+class Batch:
+    """Many independent instances advanced by one persistent launch per RK stage."""
+
+    def __init__(self, cfgs):
+        L = lib()
+        arr = (WbConfig * len(cfgs))(*cfgs)
+        self._b = ctypes.c_void_p()
+        rc = L.wb_batch_create(arr, len(cfgs), ctypes.byref(self._b))
+        if rc != WB_OK:
+            msg = L.wb_batch_last_error(self._b).decode() if self._b else "wb_batch_create failed"
+            if self._b:
+                L.wb_batch_destroy(self._b)
+            self._b = None
+            raise WbError(rc, msg)
+        self.cfgs = list(cfgs)
+
+    def _check(self, rc):
+        if rc != WB_OK:
+            raise WbError(rc, lib().wb_batch_last_error(self._b).decode())
+
+    def close(self):
+        if self._b:
+            lib().wb_batch_destroy(self._b)
+            self._b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def init_perturbation(self, ics):
+        arr = (WbPerturbation * len(ics))(*ics)
+        self._check(lib().wb_batch_init_perturbation(self._b, arr))
+
+    def step(self, nsteps=1, dt=-1.0):
+        self._check(lib().wb_batch_step(self._b, int(nsteps), float(dt)))
+
+    def sync(self):
+        self._check(lib().wb_batch_sync(self._b))
+
+    def download(self, index):
+        c = self.cfgs[index]
+        out = np.zeros((4, num_modes(c.order, c.basis), c.ny, c.nx))
+        self._check(lib().wb_batch_download(self._b, int(index), _ptr(out)))
+        return out
+
+    @property
+    def dofs(self):
+        n = ctypes.c_int64()
+        self._check(lib().wb_batch_total_dofs(self._b, ctypes.byref(n)))
+        return n.value
+
+
+# ---------------------------------------------------------------- 1D finite volume
+
+class Solver1D:
+    """compute_update / evolve of benchmark_1d.f90 (the fvm.f90 path) on the device, FP64.
+
+    State layout: delta[i, v], v = 0..2 is the (rho, rho*u, E) perturbation of cell i.
+    """
+
+    def __init__(self, nx=256, bc=BC_COPY, limiter=1, eq_kind=EQ_ISOTHERMAL, gamma=1.4, g=1.0,
+                 rho0=1.0, p0=1.0, kpoly=1.0, lx=1.0, cfl=0.4, device=0):
+        L = lib()
+        c = Wb1dConfig()
+        c.nx, c.bc, c.limiter, c.eq_kind, c.device = nx, bc, limiter, eq_kind, device
+        c.gamma, c.g, c.rho0, c.p0, c.kpoly, c.lx, c.cfl = gamma, g, rho0, p0, kpoly, lx, cfl
+        self.cfg = c
+        self._c = ctypes.c_void_p()
+        rc = L.wb1d_create(ctypes.byref(c), ctypes.byref(self._c))
+        if rc != WB_OK:
+            msg = L.wb1d_last_error(self._c).decode() if self._c else "wb1d_create failed"
+            if self._c:
+                L.wb1d_destroy(self._c)
+            self._c = None
+            raise WbError(rc, msg)
+
+    def _check(self, rc):
+        if rc != WB_OK:
+            raise WbError(rc, lib().wb1d_last_error(self._c).decode())
+
+    def close(self):
+        if self._c:
+            lib().wb1d_destroy(self._c)
+            self._c = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def upload(self, delta):
+        a = np.ascontiguousarray(delta, dtype=np.float64).reshape(self.cfg.nx, 3)
+        self._check(lib().wb1d_upload(self._c, _ptr(a)))
+
+    def download(self):
+        out = np.zeros((self.cfg.nx, 3))
+        self._check(lib().wb1d_download(self._c, _ptr(out)))
+        return out
+
+    def compute_update(self, delta):
+        a = np.ascontiguousarray(delta, dtype=np.float64).reshape(self.cfg.nx, 3)
+        out = np.zeros((self.cfg.nx, 3))
+        self._check(lib().wb1d_compute_update(self._c, _ptr(a), _ptr(out)))
+        return out
+
+    def evolve(self, tend, max_steps=10**8):
+        n = ctypes.c_int32()
+        t = ctypes.c_double()
+        self._check(lib().wb1d_evolve(self._c, float(tend), int(max_steps), ctypes.byref(n),
+                                      ctypes.byref(t)))
+        return n.value, t.value

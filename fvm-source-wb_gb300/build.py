@@ -14,8 +14,10 @@ LIB = os.path.join(OUT, "libwbgb300.so")
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
-SOURCES = ["wb_kernels_f32.cu", "wb_kernels_f64.cu", "wb_capi.cu", "wb_tables.cpp",
-           "wb_batch.cu", "wb_fv1d.cu"]
+SOURCES = ["wb_stage_f32_k2p.cu", "wb_stage_f32_k2q.cu", "wb_stage_f64_k2p.cu",
+           "wb_stage_f64_k2q.cu", "wb_kernels_f64.cu", "wb_kernels_f32.cu", "wb_stage_f32_k1p.cu",
+           "wb_stage_f32_k1q.cu", "wb_stage_f64_k1p.cu", "wb_stage_f64_k1q.cu", "wb_stage_f32_k0.cu",
+           "wb_stage_f64_k0.cu", "wb_capi.cu", "wb_batch.cu", "wb_fv1d.cu", "wb_tables.cpp"]
 
 
 def _deps():

@@ -85,7 +85,8 @@ __global__ void k_max_speed(const __grid_constant__ StageArgs<R> A, const R *u) 
       spx = spy = 0.0;
     }
   }
-  double mx = block_max(spx, red), my = block_max(spy, red);
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
+  double mx = block_max(spx, red, tid, nthr), my = block_max(spy, red, tid, nthr);
   if (threadIdx.x == 0 && threadIdx.y == 0) {
     atomicMax(&A.dev->smax[A.parity][0], (unsigned long long)__double_as_longlong(mx));
     atomicMax(&A.dev->smax[A.parity][1], (unsigned long long)__double_as_longlong(my));

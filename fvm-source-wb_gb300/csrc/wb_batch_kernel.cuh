@@ -1,0 +1,133 @@
+// wb_batch_kernel.cuh -- persistent kernels of the batched form: every CTA walks a work
+// list of (instance, tile) items spanning all instances of the batch (each with its
+// own grid, degree and equilibrium), one launch per RK stage.  Included by the FP32
+// translation unit (the batch runs the FP32-perturbation form).
+#pragma once
+#include "wb_stage.cuh"
+
+namespace wb {
+
+// item = {instance, i0, j0, (K << 24) | (TX << 12) | TY}
+__device__ __forceinline__ void unpack_item(int4 w, int &K, int &TX, int &TY) {
+  K = (w.w >> 24) & 0xff;
+  TX = (w.w >> 12) & 0xfff;
+  TY = w.w & 0xfff;
+}
+
+// The batch runs one tile shape (all instances, all degrees).
+constexpr int BATCH_TX = 32, BATCH_TY = 8;
+
+// Stage the item `it` (instance arguments copied to sA, tile staged into buf).
+template <typename R>
+__device__ __forceinline__ void item_load(const StageArgs<R> *__restrict__ args, const int4 w,
+                                          StageArgs<R> &sA, R *buf, int tid, int nthr) {
+  static_assert(sizeof(StageArgs<R>) % 4 == 0, "word copy");
+  const int *src = reinterpret_cast<const int *>(args + w.x);
+  for (int k = tid; k < (int)(sizeof(StageArgs<R>) / 4); k += nthr)
+    reinterpret_cast<int *>(&sA)[k] = src[k];
+  int K, TX, TY;
+  unpack_item(w, K, TX, TY);
+  const StageArgs<R> &A = args[w.x];
+  const bool lim = A.limiter && A.lim_y && K >= 1;
+  if (K == 0) tile_load_async<R, 0, 1, BATCH_TX, BATCH_TY>(A, lim, w.y, w.z, buf, tid);
+  else if (K == 1) tile_load_async<R, 1, 1, BATCH_TX, BATCH_TY>(A, lim, w.y, w.z, buf, tid);
+  else tile_load_async<R, 2, 1, BATCH_TX, BATCH_TY>(A, lim, w.y, w.z, buf, tid);
+}
+
+// Persistent batched stage: CTAs stride over the work list; the next-but-one item is
+// staged (cp.async) while the current one is computed.  bufsz = the largest tile buffer.
+template <typename R>
+__global__ void __launch_bounds__(256, 2)
+    k_batch_stage(const StageArgs<R> *__restrict__ args, const int4 *__restrict__ items, int nitems,
+                  int bufsz) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(16) StageArgs<R> sA[2];  // instance arguments of the staged items
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  double *red = reinterpret_cast<double *>(smem_raw);
+  R *bufs = reinterpret_cast<R *>(smem_raw + 64 * sizeof(double));
+  R *flux = bufs + 2 * bufsz;
+  int it = blockIdx.x;
+  if (it < nitems) item_load(args, items[it], sA[0], bufs, tid, nthr);
+  cp_async_commit();
+  if (it + (int)gridDim.x < nitems) item_load(args, items[it + gridDim.x], sA[1], bufs + bufsz, tid, nthr);
+  cp_async_commit();
+  for (int k = 0; it < nitems; it += gridDim.x, ++k) {
+    cp_async_wait<1>();
+    __syncthreads();
+    const int4 w = items[it];
+    int K, TX, TY;
+    unpack_item(w, K, TX, TY);
+    const StageArgs<R> &A = sA[k & 1];
+    R *buf = bufs + (k & 1) * bufsz;
+    const double dt = stage_dt(A);
+    if (A.advance_time && w.y == 0 && w.z == 0 && tid == 0) {
+      DevState *S = A.dev;
+      S->t[A.parity ^ 1] = S->t[A.parity] + dt;
+      S->nstep[A.parity ^ 1] = S->nstep[A.parity] + (dt > 0.0 ? 1 : 0);
+      S->smax[A.parity ^ 1][0] = 0ull;
+      S->smax[A.parity ^ 1][1] = 0ull;
+    }
+    const bool lim = A.limiter && A.lim_y && K >= 1;
+    if (K == 0) tile_compute<R, 0, 1, BATCH_TX, BATCH_TY>(A, lim, w.y, w.z, buf, flux, red, tid, dt);
+    else if (K == 1) tile_compute<R, 1, 1, BATCH_TX, BATCH_TY>(A, lim, w.y, w.z, buf, flux, red, tid, dt);
+    else tile_compute<R, 2, 1, BATCH_TX, BATCH_TY>(A, lim, w.y, w.z, buf, flux, red, tid, dt);
+    const int in = it + 2 * (int)gridDim.x;
+    if (in < nitems) item_load(args, items[in], sA[k & 1], buf, tid, nthr);
+    cp_async_commit();
+  }
+  cp_async_wait<0>();
+}
+
+// Per-instance wave-speed maxima of the cell means into dev->smax[parity] (the batched
+// compute_max_speed), over the same work list.
+template <typename R>
+__global__ void __launch_bounds__(256)
+    k_batch_max_speed(const StageArgs<R> *__restrict__ args, const R *const *__restrict__ state,
+                      const int4 *__restrict__ items, int nitems) {
+  __shared__ double red[64];
+  const int tid = threadIdx.x;
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const int4 w = items[it];
+    int K, TX, TY;
+    unpack_item(w, K, TX, TY);
+    const StageArgs<R> &A = args[w.x];
+    const R *u = state[w.x];
+    const int NQ = K + 1, NB = num_modes(K, 1);
+    const Tab1D<R> &T = c_tab[K];
+    const int gi = w.y + tid % TX, gj = w.z + tid / TX;
+    double spx = 0.0, spy = 0.0;
+    if (gi < A.nx && gj < A.ny) {
+      const long long cell = (long long)gj * A.nx + gi;
+      R rbar = R(0), pbar = R(0);
+      for (int qa = 0; qa < NQ; ++qa)
+        for (int qb = 0; qb < NQ; ++qb) {
+          R re, pe;
+          eq_point(A, A.fxv[gi * NQ + qa], A.fyv[gj * NQ + qb], re, pe);
+          R ww = R(0.25) * T.wq[qa] * T.wq[qb];
+          rbar += re * ww;
+          pbar += pe * ww;
+        }
+      R d0 = u[(long long)(0 * NB) * A.plane + cell], d1 = u[(long long)(1 * NB) * A.plane + cell];
+      R d2 = u[(long long)(2 * NB) * A.plane + cell], d3 = u[(long long)(3 * NB) * A.plane + cell];
+      R rf = rfmax(rbar + d0, R(1.0e-9f));
+      R inv = R(1) / rf;
+      R vx = d1 * inv, vy = d2 * inv;
+      R p = pbar + A.gm1 * (d3 - R(0.5) * (d1 * vx + d2 * vy));
+      R cs = sqrt(A.gamma * rfmax(p, R(1e-10)) / rfmax(rf, R(1e-10)));
+      spx = (double)(fabs(vx) + cs);
+      spy = (double)(fabs(vy) + cs);
+      if (!isfinite(spx) || !isfinite(spy)) {
+        atomicOr(&A.dev->err, 1);
+        spx = spy = 0.0;
+      }
+    }
+    double mx = block_max(spx, red, tid, blockDim.x);
+    double my = block_max(spy, red, tid, blockDim.x);
+    if (tid == 0) {
+      atomicMax(&A.dev->smax[A.parity][0], (unsigned long long)__double_as_longlong(mx));
+      atomicMax(&A.dev->smax[A.parity][1], (unsigned long long)__double_as_longlong(my));
+    }
+  }
+}
+
+}  // namespace wb

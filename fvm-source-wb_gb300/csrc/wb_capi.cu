@@ -80,8 +80,9 @@ int validate(const wb_config *c, std::string &why) {
   if (c->tile_x < 0 || c->tile_y < 0) return why = "bad tile", WB_ERR_CONFIG;
   if (c->tile_x > 0 || c->tile_y > 0) {
     long long t = (long long)c->tile_x * c->tile_y;
-    if (c->tile_x < 1 || c->tile_y < 1 || t > 1024 || t < 32 || (t % 32) != 0)
-      return why = "tile_x*tile_y must be a multiple of 32 in [32,1024]", WB_ERR_CONFIG;
+    if (!tile_supported(c->precision == WB_PREC_FP32, c->tile_x, c->tile_y))
+      return why = "tile shape not compiled (FP32: 32x8, 16x16; FP64: 16x8)", WB_ERR_CONFIG;
+    (void)t;
   }
   return WB_OK;
 }
@@ -556,8 +557,7 @@ int wb_create(const wb_config *cfg, wb_ctx **out) {
   Tab1D<float> t32[KMAX + 1];
   make_tab1d(t64);
   convert_tabs<float>(t64, t32, KMAX + 1);
-  CK(upload_tables(t64));
-  CK(upload_tables(t32));
+  CK(upload_tables(t32, t64));
   if ((rc = dalloc(ctx, &ctx->Td, sizeof(t64)))) return rc;
   CK(cudaMemcpy(ctx->Td, t64, sizeof(t64), cudaMemcpyHostToDevice));
   // equilibrium factor tables
@@ -803,6 +803,78 @@ int wb_get_time(wb_ctx *ctx, double *t, int64_t *steps) {
   return WB_OK;
 }
 
+// Fortran 1PE12.5: one digit before the point, five after, exponent E+dd (or +ddd with
+// the E dropped when the exponent needs three digits), right-justified in 12 columns.
+static void fortran_1pe12_5(double v, char *out) {
+  char buf[64];
+  std::snprintf(buf, sizeof(buf), "%.5E", v);
+  char *e = std::strchr(buf, 'E');
+  if (e) {
+    int ex = std::atoi(e + 1);
+    if (ex >= 100 || ex <= -100) std::snprintf(e, 8, "%c%03d", ex < 0 ? '-' : '+', ex < 0 ? -ex : ex);
+  }
+  std::snprintf(out, 16, "%12s", buf);
+}
+
+int wb_write_dat(wb_ctx *ctx, const char *path, int32_t var) {
+  if (!ctx || !path || var < 1 || var > 4) return WB_ERR_ARG;
+  const wb_config &g = ctx->cfg;
+  std::vector<double> d((size_t)NV * ctx->nb * ctx->ncell);
+  int rc = wb_download_state(ctx, d.data(), WB_LAYOUT_SOA);
+  if (rc) return rc;
+  Tab1D<double> t64[KMAX + 1];
+  make_tab1d(t64);
+  const Tab1D<double> &T = t64[g.order];
+  EqParams ep{g.eq_kind, g.gamma, g.gx, g.gy, g.rho0, g.p0, g.kpoly};
+  const double dx = g.lx / g.nx, dy = g.ly / g.ny, gm1 = g.gamma - 1.0;
+  FILE *f = std::fopen(path, "w");
+  if (!f) return set_err(ctx, WB_ERR_ARG, std::string("cannot open ") + path);
+  char num[16];
+  for (int i = 0; i < g.nx; ++i)
+    for (int j = 0; j < g.ny; ++j) {
+      const size_t cell = (size_t)j * g.nx + i;
+      const double x = ((double)i + 0.5) * dx + dx / 2.0 * T.xq[0];
+      const double y = ((double)j + 0.5) * dy + dy / 2.0 * T.xq[0];
+      double re, pe;
+      eq_combine(ep, eq_factor_x(ep, x), eq_factor_y(ep, y), &re, &pe);
+      double u[NV];
+      for (int v = 0; v < NV; ++v) {
+        double s = 0.0;
+        for (int m = 0; m < ctx->nb; ++m)
+          s += d[((size_t)v * ctx->nb + m) * ctx->ncell + cell] *
+               T.B[mode_deg(g.order, g.basis, m, 0)][0] * T.B[mode_deg(g.order, g.basis, m, 1)][0];
+        u[v] = s;
+      }
+      const double rho = re + u[0], vx = u[1] / rho, vy = u[2] / rho;
+      const double p = gm1 * (pe / gm1 + u[3] - 0.5 * rho * (vx * vx + vy * vy));
+      const double w[NV] = {rho - re, vx, vy, p - pe};
+      fortran_1pe12_5(x, num);
+      std::fprintf(f, "%s ", num);
+      fortran_1pe12_5(y, num);
+      std::fprintf(f, "%s ", num);
+      for (int v = var - 1; v < NV; ++v) {
+        fortran_1pe12_5(w[v], num);
+        std::fprintf(f, "%s ", num);
+      }
+      std::fprintf(f, "\n");
+    }
+  std::fclose(f);
+  return WB_OK;
+}
+
+int wb_set_time(wb_ctx *ctx, double t, int64_t steps) {
+  if (!ctx || !(t >= 0.0) || steps < 0) return WB_ERR_ARG;
+  CK(cudaSetDevice(ctx->cfg.device));
+  DevState h;
+  CK(cudaMemcpyAsync(&h, ctx->dev, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  h.t[ctx->parity] = t;
+  h.nstep[ctx->parity] = steps;
+  CK(cudaMemcpyAsync(ctx->dev, &h, sizeof(h), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return WB_OK;
+}
+
 int wb_evolve(wb_ctx *ctx, double tend, int32_t max_steps, int32_t *steps_done, double *t_out) {
   if (!ctx || max_steps < 0) return WB_ERR_ARG;
   CK(cudaSetDevice(ctx->cfg.device));
@@ -902,3 +974,52 @@ int wb_conserved_sums(wb_ctx *ctx, double sums[4]) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------ context internals for the batch
+namespace wb {
+
+int ctx_rk2_stage_args(wb_ctx *ctx, int phase, int dt_mode, double dt, StageArgs<float> out[2]) {
+  if (!is_fp32(ctx) || ctx->cfg.integrator != WB_RK2) return WB_ERR_CONFIG;
+  const int cur0 = ctx->cur, par0 = ctx->parity;
+  ctx->cur = (cur0 + 2 * phase) % ctx->nbuf;
+  ctx->parity = (par0 + phase) & 1;
+  StageArgs<float> A = base_args<float>(ctx);
+  A.dt_mode = dt_mode;
+  A.dt_fixed = dt;
+  float *U = (float *)state_buf(ctx, 0), *W1 = (float *)state_buf(ctx, 1);
+  float *Un = (float *)state_buf(ctx, 2);
+  out[0] = A;
+  out[0].x = U;
+  out[0].o[0].out = W1;
+  out[0].o[0].beta = 1.0f;
+  out[0].o[0].cdt = 1.0f;
+  out[0].advance_time = 1;
+  out[1] = A;
+  out[1].x = W1;
+  out[1].o[0].out = Un;
+  out[1].o[0].in[0] = U;
+  out[1].o[0].c[0] = 0.5f;
+  out[1].o[0].lim[0] = 1;
+  out[1].o[0].beta = 0.5f;
+  out[1].o[0].cdt = 0.5f;
+  out[1].compute_speed = 1;
+  ctx->cur = cur0;
+  ctx->parity = par0;
+  return WB_OK;
+}
+const float *ctx_state_f32(wb_ctx *c) { return (const float *)state_buf(c, 0); }
+DevState *ctx_dev_state(wb_ctx *c) { return c->dev; }
+void ctx_tile(wb_ctx *c, int *tx, int *ty) {
+  *tx = c->TX;
+  *ty = c->TY;
+}
+void ctx_advance(wb_ctx *c, int n) {
+  c->cur = (c->cur + 2 * n) % c->nbuf;
+  c->parity = (c->parity + n) & 1;
+}
+void ctx_set_speed_valid(wb_ctx *c, bool v) { c->speed_valid = v; }
+bool ctx_speed_valid(wb_ctx *c) { return c->speed_valid; }
+int ctx_parity(wb_ctx *c) { return c->parity; }
+size_t ctx_dofs(wb_ctx *c) { return (size_t)NV * c->nb * c->ncell; }
+
+}  // namespace wb

@@ -6,9 +6,7 @@
 namespace wb {
 
 #define WB_DECLARE_PRECISION_ENTRY_POINTS(R)                                                   \
-  cudaError_t upload_tables(const Tab1D<R> *t);                                                \
-  cudaError_t launch_stage(const StageArgs<R> &A, int K, int basis, int TX, int TY,            \
-                           cudaStream_t s);                                                    \
+  cudaError_t upload_tables_aux(const Tab1D<R> *t);                                            \
   cudaError_t launch_limit(const StageArgs<R> &A, R *u, int K, int basis, cudaStream_t s);     \
   cudaError_t launch_max_speed(const StageArgs<R> &A, const R *u, int K, int basis,            \
                                cudaStream_t s);                                                \
@@ -24,12 +22,90 @@ namespace wb {
 WB_DECLARE_PRECISION_ENTRY_POINTS(float)
 WB_DECLARE_PRECISION_ENTRY_POINTS(double)
 
+// stage translation units (one per precision, degree and basis)
+#define WB_DECLARE_STAGE_TU(R, TAG)                                                             \
+  cudaError_t upload_tables_##TAG(const Tab1D<R> *t);                                          \
+  cudaError_t launch_stage_##TAG(const StageArgs<R> &A, int TX, int TY, cudaStream_t s);
+WB_DECLARE_STAGE_TU(float, f32_k0)
+WB_DECLARE_STAGE_TU(float, f32_k1q)
+WB_DECLARE_STAGE_TU(float, f32_k1p)
+WB_DECLARE_STAGE_TU(float, f32_k2q)
+WB_DECLARE_STAGE_TU(float, f32_k2p)
+WB_DECLARE_STAGE_TU(double, f64_k0)
+WB_DECLARE_STAGE_TU(double, f64_k1q)
+WB_DECLARE_STAGE_TU(double, f64_k1p)
+WB_DECLARE_STAGE_TU(double, f64_k2q)
+WB_DECLARE_STAGE_TU(double, f64_k2p)
+
+inline cudaError_t launch_stage(const StageArgs<float> &A, int K, int basis, int TX, int TY,
+                                cudaStream_t s) {
+  if (K == 0) return launch_stage_f32_k0(A, TX, TY, s);
+  if (K == 1) return basis == 0 ? launch_stage_f32_k1q(A, TX, TY, s) : launch_stage_f32_k1p(A, TX, TY, s);
+  return basis == 0 ? launch_stage_f32_k2q(A, TX, TY, s) : launch_stage_f32_k2p(A, TX, TY, s);
+}
+inline cudaError_t launch_stage(const StageArgs<double> &A, int K, int basis, int TX, int TY,
+                                cudaStream_t s) {
+  if (K == 0) return launch_stage_f64_k0(A, TX, TY, s);
+  if (K == 1) return basis == 0 ? launch_stage_f64_k1q(A, TX, TY, s) : launch_stage_f64_k1p(A, TX, TY, s);
+  return basis == 0 ? launch_stage_f64_k2q(A, TX, TY, s) : launch_stage_f64_k2p(A, TX, TY, s);
+}
+// Uploads the basis tables to the constant memory of every translation unit.
+inline cudaError_t upload_tables(const Tab1D<float> *t32, const Tab1D<double> *t64) {
+  cudaError_t (*f32[])(const Tab1D<float> *) = {upload_tables_aux, upload_tables_f32_k0,
+                                                upload_tables_f32_k1q, upload_tables_f32_k1p,
+                                                upload_tables_f32_k2q, upload_tables_f32_k2p};
+  cudaError_t (*f64[])(const Tab1D<double> *) = {upload_tables_aux, upload_tables_f64_k0,
+                                                 upload_tables_f64_k1q, upload_tables_f64_k1p,
+                                                 upload_tables_f64_k2q, upload_tables_f64_k2p};
+  for (auto f : f32) {
+    cudaError_t e = f(t32);
+    if (e != cudaSuccess) return e;
+  }
+  for (auto f : f64) {
+    cudaError_t e = f(t64);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+// Tile shapes the stage kernels are compiled for.
+inline bool tile_supported(int precision_fp32, int tx, int ty) {
+  if (precision_fp32) return (tx == 32 && ty == 8) || (tx == 16 && ty == 16);
+  return tx == 16 && ty == 8;
+}
+
 // FP64-only diagnostics and precision conversion (defined in wb_kernels_f64.cu)
 cudaError_t launch_norms(const AuxArgs &A, const Tab1D<double> *Td, const double *a,
                          const double *b, double *partial, double *out, int K, int basis,
                          cudaStream_t s);
 cudaError_t launch_f32_to_f64(double *out, const float *in, long long n, cudaStream_t s);
 cudaError_t launch_f64_to_f32(float *out, const double *in, long long n, cudaStream_t s);
+
+// batched form (FP32): persistent stage over a work list; per-instance max speed
+cudaError_t launch_batch_stage(const StageArgs<float> *args, const int4 *items, int nitems,
+                               int bufsz, size_t smem, int *grid_out, cudaStream_t s);
+cudaError_t launch_batch_max_speed(const StageArgs<float> *args, const float *const *state,
+                                   const int4 *items, int nitems, cudaStream_t s);
+
+}  // namespace wb
+
+// Context internals used by the batched form (defined in wb_capi.cu).
+struct wb_ctx;
+namespace wb {
+// RK2 stage arguments of a context for step phase p (0..5: buffer rotation mod 3 and
+// parity mod 2, counted from the context's current position); FP32 contexts only.
+int ctx_rk2_stage_args(wb_ctx *c, int phase, int dt_mode, double dt, StageArgs<float> out[2]);
+// device address of the current state and of the context's run state
+const float *ctx_state_f32(wb_ctx *c);
+DevState *ctx_dev_state(wb_ctx *c);
+// tile shape chosen for the context
+void ctx_tile(wb_ctx *c, int *tx, int *ty);
+// advance the host-side buffer rotation / parity bookkeeping by n RK2 steps
+void ctx_advance(wb_ctx *c, int n);
+// mark the fused wave-speed maxima of the current state as valid
+void ctx_set_speed_valid(wb_ctx *c, bool v);
+bool ctx_speed_valid(wb_ctx *c);
+int ctx_parity(wb_ctx *c);
+size_t ctx_dofs(wb_ctx *c);
 
 // bytes of the partial-sum buffer the diagnostics need for an nx x ny grid
 size_t diag_partial_bytes(int nx, int ny);

@@ -21,24 +21,6 @@ static inline dim3 cell_grid(int nx, int ny, dim3 blk) {
 }
 
 template <typename R>
-static cudaError_t launch_stage_t(const StageArgs<R> &A, int K_, int B_, int TX, int TY,
-                                  cudaStream_t s) {
-  const int lim = A.limiter && A.lim_y && K_ >= 1;
-  const size_t smem = stage_smem_bytes<R>(K_, B_, TX, TY, lim);
-  dim3 blk(TX, TY), grd = cell_grid(A.nx, A.ny, blk);
-  cudaError_t e = cudaSuccess;
-  WB_DISPATCH_KB(K_, B_, {
-    auto kern = k_stage<R, K, BASIS>;
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess) {
-      kern<<<grd, blk, smem, s>>>(A);
-      e = cudaGetLastError();
-    }
-  });
-  return e;
-}
-
-template <typename R>
 static cudaError_t launch_limit_t(const StageArgs<R> &A, R *u, int K_, int B_, cudaStream_t s) {
   if (K_ < 1) return cudaSuccess;
   dim3 blk(32, 8), grd = cell_grid(A.nx, A.ny, blk);
@@ -96,12 +78,8 @@ static cudaError_t launch_sums_t(const AuxArgs &A, const Tab1D<double> *Td, cons
 // Defines the exported per-precision entry points declared in wb_internal.h.
 #define WB_DEFINE_PRECISION_ENTRY_POINTS(R)                                                    \
   namespace wb {                                                                               \
-  cudaError_t upload_tables(const Tab1D<R> *t) {                                               \
+  cudaError_t upload_tables_aux(const Tab1D<R> *t) {                                           \
     return cudaMemcpyToSymbol(c_tab, t, sizeof(Tab1D<R>) * (KMAX + 1));                       \
-  }                                                                                            \
-  cudaError_t launch_stage(const StageArgs<R> &A, int K, int basis, int TX, int TY,            \
-                           cudaStream_t s) {                                                   \
-    return launch_stage_t<R>(A, K, basis, TX, TY, s);                                          \
   }                                                                                            \
   cudaError_t launch_limit(const StageArgs<R> &A, R *u, int K, int basis, cudaStream_t s) {    \
     return launch_limit_t<R>(A, u, K, basis, s);                                               \

@@ -41,6 +41,13 @@ __device__ __forceinline__ int wrap_index(int i, int n, int bc) {
 template <typename R>
 __device__ __forceinline__ R rfmax(R a, R b) { return a > b ? a : b; }
 
+// Reciprocal and square root of the FP32 perturbation form: the hardware approximations
+// (MUFU, about 1 ulp), well inside the form's 1e-6 error budget.  FP64 stays IEEE.
+__device__ __forceinline__ float frcp(float x) { return __fdividef(1.0f, x); }
+__device__ __forceinline__ double frcp(double x) { return 1.0 / x; }
+__device__ __forceinline__ float fsqrt_pos(float x) { return x * rsqrtf(x); }
+__device__ __forceinline__ double fsqrt_pos(double x) { return sqrt(x); }
+
 // minmod / generalized minmod of 2d/limiters.f90:18-54
 template <typename R>
 __device__ __forceinline__ R minmod3(R x, R y, R z) {
@@ -114,15 +121,17 @@ __device__ __forceinline__ void vol_point(const StageArgs<R> &A, const R *d, R r
     flux_lit<1>(ue, we, fe);
 #pragma unroll
     for (int v = 0; v < NV; ++v) Fy[v] = (f[v] - fe[v]) * A.hidy;
+    // rounded products (never contracted into the subtraction below): S(u_eq + 0) and
+    // S(u_eq) must round identically so a zero perturbation cancels exactly
     double s[NV], se[NV];
     s[0] = 0.0;
-    s[1] = -(w[0] * A.gx);
-    s[2] = -(w[0] * A.gy);
-    s[3] = -(w[0] * (w[1] * A.gx + w[2] * A.gy));
+    s[1] = -__dmul_rn(w[0], A.gx);
+    s[2] = -__dmul_rn(w[0], A.gy);
+    s[3] = -__dmul_rn(w[0], __dadd_rn(__dmul_rn(w[1], A.gx), __dmul_rn(w[2], A.gy)));
     se[0] = 0.0;
-    se[1] = -(we[0] * A.gx);
-    se[2] = -(we[0] * A.gy);
-    se[3] = -(we[0] * (we[1] * A.gx + we[2] * A.gy));
+    se[1] = -__dmul_rn(we[0], A.gx);
+    se[2] = -__dmul_rn(we[0], A.gy);
+    se[3] = -__dmul_rn(we[0], __dadd_rn(__dmul_rn(we[1], A.gx), __dmul_rn(we[2], A.gy)));
 #pragma unroll
     for (int v = 0; v < NV; ++v) S[v] = (s[v] - se[v]) * 0.25;
   } else {
@@ -131,7 +140,7 @@ __device__ __forceinline__ void vol_point(const StageArgs<R> &A, const R *d, R r
     //   d(u (E+p)) = u (H_eq + dE + dp), dp = (gamma-1)(dE - |m|^2/(2 rho)),
     //   dS = (0, -drho gx, -drho gy, -(m_x gx + m_y gy))
     R r = rfmax(re + d[0], R(1.0e-9f));
-    R inv = R(1) / r;
+    R inv = frcp(r);
     R vx = d[1] * inv, vy = d[2] * inv;
     R dp = A.gm1 * (d[3] - R(0.5) * (d[1] * vx + d[2] * vy));
     R H = A.hgam * pe + d[3] + dp;
@@ -187,7 +196,7 @@ __device__ __forceinline__ void face_point(const StageArgs<R> &A, const R *dL, c
       const R *d = s == 0 ? dL : dR;
       R *f = s == 0 ? fL : fR;
       R r = rfmax(re + d[0], R(1.0e-9f));
-      R inv = R(1) / r;
+      R inv = frcp(r);
       R vx = d[1] * inv, vy = d[2] * inv;
       R dp = A.gm1 * (d[3] - R(0.5) * (d[1] * vx + d[2] * vy));
       R H = hp + d[3] + dp;
@@ -196,7 +205,7 @@ __device__ __forceinline__ void face_point(const StageArgs<R> &A, const R *dL, c
       f[1] = DIR == 0 ? d[1] * vx + dp : d[1] * vy;
       f[2] = DIR == 0 ? d[2] * vx : d[2] * vy + dp;
       f[3] = vn * H;
-      R c = sqrt(A.gamma * rfmax(pe + dp, R(1e-10)) * inv);
+      R c = fsqrt_pos(A.gamma * rfmax(pe + dp, R(1e-10)) * inv);
       R lam = A.llf_speed == 1 ? vn + c : fabs(vn) + c;
       if (s == 0) lamL = lam; else lamR = lam;
     }
@@ -226,10 +235,9 @@ __device__ __forceinline__ void limit_modes(const StageArgs<R> &A, R *base, int 
   }
 }
 
-__device__ __forceinline__ double block_max(double v, double *red) {
+__device__ __forceinline__ double block_max(double v, double *red, int tid, int nthr) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-  int nthr = blockDim.x * blockDim.y, tid = threadIdx.y * blockDim.x + threadIdx.x;
   int warp = tid >> 5, lane = tid & 31;
   if (lane == 0) red[warp] = v;
   __syncthreads();
@@ -256,63 +264,103 @@ __device__ __forceinline__ double stage_dt(const StageArgs<R> &A) {
   return dt;
 }
 
-// Shared-memory bytes for a TX x TY tile.
-template <typename R>
-__host__ __device__ inline size_t stage_smem_bytes(int K, int basis, int TX, int TY, int lim) {
-  int NB = num_modes(K, basis), NQ = K + 1;
-  size_t n = (size_t)NV * NB * (TY + 2) * (TX + 2);
-  if (lim) n += (size_t)NV * (TY + 4) * (TX + 4);
-  n += (size_t)NV * NQ * TY * (TX + 1) + (size_t)NV * NQ * (TY + 1) * TX;
-  return n * sizeof(R) + 64 * sizeof(double);
+// ---------------------------------------------------------------- tile staging
+
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void *smem, const void *gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(s), "l"(gmem), "n"(BYTES));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+// Issue the asynchronous copies that stage one tile (lower-left cell (i0, j0)) into `buf`:
+// the modes of the tile and a one-cell halo, the means of a two-cell halo when the
+// limiter is on, and the tile's equilibrium factors.  Boundary conditions are applied by
+// index mapping.  Warps copy whole rows (no per-element division).
+template <typename R, int K, int BASIS, int TX, int TY>
+__device__ __forceinline__ void tile_load_async(const StageArgs<R> &A, const bool lim,
+                                                const int i0, const int j0, R *buf,
+                                                const int tid) {
+  constexpr int nthr = TX * TY;
+  const TileLayout L = tile_layout(K, BASIS, TX, TY, lim);
+  const int lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
+  const int nx = A.nx, ny = A.ny;
+  const long long P = A.plane;
+  int gc[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) gc[k] = wrap_index(i0 + lane + 32 * k - 1, nx, A.bc_x);
+  const int nrow = NV * L.NB * L.RY;
+  for (int row = warp; row < nrow; row += nwarp) {
+    const int pl = row / L.RY, ry = row - pl * L.RY;
+    const int gj = wrap_index(j0 + ry - 1, ny, A.bc_y);
+    const R *src = A.x + pl * P + (long long)gj * nx;
+    R *dst = buf + L.su + row * L.RX;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int c = lane + 32 * k;
+      if (c < L.RX) cp_async<sizeof(R)>(dst + c, src + gc[k]);
+    }
+  }
+  if (L.lim) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) gc[k] = wrap_index(i0 + lane + 32 * k - 2, nx, A.bc_x);
+    const int mrow = NV * L.LY;
+    for (int row = warp; row < mrow; row += nwarp) {
+      const int v = row / L.LY, ly = row - v * L.LY;
+      const int gj = wrap_index(j0 + ly - 2, ny, A.bc_y);
+      const R *src = A.x + (long long)(v * L.NB) * P + (long long)gj * nx;
+      R *dst = buf + L.sm + row * L.LX;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const int c = lane + 32 * k;
+        if (c < L.LX) cp_async<sizeof(R)>(dst + c, src + gc[k]);
+      }
+    }
+  }
+  // equilibrium factors: fxv [NQ*TX], fxf [TX+1], fyv [NQ*TY], fyf [TY+1] (indices clamped)
+  const int NQ = L.NQ;
+  const int n1 = NQ * TX, n2 = n1 + TX + 1, n3 = n2 + NQ * TY, n4 = n3 + TY + 1;
+  R *e = buf + L.eq;
+  for (int k = tid; k < n4; k += nthr) {
+    const R *src;
+    if (k < n1) src = A.fxv + min(i0 * NQ + k, nx * NQ - 1);
+    else if (k < n2) src = A.fxf + min(i0 + (k - n1), nx);
+    else if (k < n3) src = A.fyv + min(j0 * NQ + (k - n2), ny * NQ - 1);
+    else src = A.fyf + min(j0 + (k - n3), ny);
+    cp_async<sizeof(R)>(e + k, src);
+  }
 }
 
-template <typename R, int K, int BASIS>
-__global__ void __launch_bounds__(256, std::is_same<R, float>::value ? 2 : 1)
-    k_stage(const __grid_constant__ StageArgs<R> A) {
+// Compute one staged tile: limiter, face fluxes, cell quadrature, RK combination and the
+// wave-speed reduction.  Thread tid owns cell (tid % TX, tid / TX).  Ends with a CTA
+// barrier, after which `buf` and the flux area may be reused.
+template <typename R, int K, int BASIS, int TX, int TY>
+__device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool lim_,
+                                             const int i0, const int j0, R *buf, R *flux,
+                                             double *red, const int tid, const double dt) {
   constexpr int NQ = K + 1;
   constexpr int NB = num_modes(K, BASIS);
   const Tab1D<R> &T = c_tab[K];
-  const int TX = blockDim.x, TY = blockDim.y;
-  const int RX = TX + 2, RY = TY + 2, RXY = RX * RY;
-  const int LX = TX + 4, LY = TY + 4;
-  const int tid = threadIdx.y * TX + threadIdx.x, nthr = TX * TY;
-  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+  const TileLayout L = tile_layout(K, BASIS, TX, TY, lim_);
+  const int RX = L.RX, RY = L.RY, RXY = L.RXY;
+  const int LX = L.LX, LY = L.LY;
+  constexpr int nthr = TX * TY;
   const int nx = A.nx, ny = A.ny;
   const long long P = A.plane;
-  const bool lim = A.limiter && A.lim_y && K >= 1;
-
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  double *red = reinterpret_cast<double *>(smem_raw);
-  R *su = reinterpret_cast<R *>(smem_raw + 64 * sizeof(double));
-  R *sm = su + NV * NB * RXY;
-  R *sfx = sm + (lim ? NV * LY * LX : 0);
+  const bool lim = lim_;
+  (void)RY;
+  R *su = buf + L.su;
+  R *sm = buf + L.sm;
+  const R *sfxv = buf + L.eq;
+  const R *sfxf = sfxv + NQ * TX;
+  const R *sfyv = sfxf + TX + 1;
+  const R *sfyf = sfyv + NQ * TY;
+  R *sfx = flux;
   const int FXS = TY * (TX + 1);
   R *sfy = sfx + NV * NQ * FXS;
   const int FYS = (TY + 1) * TX;
-
-  const double dt = stage_dt(A);
-  if (A.advance_time && blockIdx.x == 0 && blockIdx.y == 0 && tid == 0) {
-    DevState *S = A.dev;
-    S->t[A.parity ^ 1] = S->t[A.parity] + dt;
-    S->nstep[A.parity ^ 1] = S->nstep[A.parity] + 1;
-    S->smax[A.parity ^ 1][0] = 0ull;
-    S->smax[A.parity ^ 1][1] = 0ull;
-  }
-
-  // 1. stage modes of the tile + one-cell halo (BC-mapped), and halo-2 means
-  for (int e = tid; e < NV * NB * RXY; e += nthr) {
-    int rx = e % RX, t1 = e / RX, ry = t1 % RY, pl = t1 / RY;
-    int gi = wrap_index(i0 + rx - 1, nx, A.bc_x), gj = wrap_index(j0 + ry - 1, ny, A.bc_y);
-    su[e] = A.x[pl * P + (long long)gj * nx + gi];
-  }
-  if (lim) {
-    for (int e = tid; e < NV * LY * LX; e += nthr) {
-      int lx = e % LX, t1 = e / LX, ly = t1 % LY, v = t1 / LY;
-      int gi = wrap_index(i0 + lx - 2, nx, A.bc_x), gj = wrap_index(j0 + ly - 2, ny, A.bc_y);
-      sm[e] = A.x[(long long)(v * NB) * P + (long long)gj * nx + gi];
-    }
-  }
-  __syncthreads();
 
   // 2. limiter on every staged cell (means never change, so cells are independent)
   if (lim) {
@@ -326,11 +374,15 @@ __global__ void __launch_bounds__(256, std::is_same<R, float>::value ? 2 : 1)
     __syncthreads();
   }
 
-  // 3a. x faces: (TX+1) x TY, face fi sits between tile cells fi-1 and fi
-  for (int f = tid; f < FXS; f += nthr) {
+  // 3. faces, x and y in one balanced loop: x face (fi, fj) sits between tile cells
+  //    fi-1 and fi of row fj; y face (fi, fj) between rows fj-1 and fj of column fi
+  for (int fa = tid; fa < FXS + FYS; fa += nthr) {
+    if (fa < FXS) {
+    const int f = fa;
     int fi = f % (TX + 1), fj = f / (TX + 1);
     int gfi = i0 + fi, gj = j0 + fj;
     if (gfi > nx || gj >= ny) continue;
+    (void)gj;
     R cl[NV][NQ], cr[NV][NQ];
 #pragma unroll
     for (int v = 0; v < NV; ++v)
@@ -350,7 +402,7 @@ __global__ void __launch_bounds__(256, std::is_same<R, float>::value ? 2 : 1)
         cl[v][b] = sl;
         cr[v][b] = sr;
       }
-    const R fxf = A.fxf[gfi];
+    const R fxf = sfxf[fi];
 #pragma unroll
     for (int q = 0; q < NQ; ++q) {
       R dL[NV], dR[NV], F[NV], re, pe;
@@ -365,14 +417,13 @@ __global__ void __launch_bounds__(256, std::is_same<R, float>::value ? 2 : 1)
         dL[v] = sl;
         dR[v] = sr;
       }
-      eq_point(A, fxf, A.fyv[gj * NQ + q], re, pe);
+      eq_point(A, fxf, sfyv[fj * NQ + q], re, pe);
       face_point<R, 0>(A, dL, dR, re, pe, F);
 #pragma unroll
       for (int v = 0; v < NV; ++v) sfx[(v * NQ + q) * FXS + f] = F[v];
     }
-  }
-  // 3b. y faces: TX x (TY+1), face fj sits between tile cells fj-1 and fj
-  for (int f = tid; f < FYS; f += nthr) {
+    } else {
+    const int f = fa - FXS;
     int fi = f % TX, fj = f / TX;
     int gi = i0 + fi, gfj = j0 + fj;
     if (gi >= nx || gfj > ny) continue;
@@ -393,7 +444,7 @@ __global__ void __launch_bounds__(256, std::is_same<R, float>::value ? 2 : 1)
         cb[v][a] = sb;
         ct[v][a] = st;
       }
-    const R fyf = A.fyf[gfj];
+    const R fyf = sfyf[fj];
 #pragma unroll
     for (int q = 0; q < NQ; ++q) {
       R dB[NV], dT[NV], F[NV], re, pe;
@@ -408,16 +459,17 @@ __global__ void __launch_bounds__(256, std::is_same<R, float>::value ? 2 : 1)
         dB[v] = sb;
         dT[v] = st;
       }
-      eq_point(A, A.fxv[gi * NQ + q], fyf, re, pe);
+      eq_point(A, sfxv[fi * NQ + q], fyf, re, pe);
       face_point<R, 1>(A, dB, dT, re, pe, F);
 #pragma unroll
       for (int v = 0; v < NV; ++v) sfy[(v * NQ + q) * FYS + f] = F[v];
+    }
     }
   }
   __syncthreads();
 
   // 4. cells
-  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int tx = tid % TX, ty = tid / TX;
   const int gi = i0 + tx, gj = j0 + ty;
   const bool active = gi < nx && gj < ny;
   double spx = 0.0, spy = 0.0;
@@ -445,7 +497,7 @@ __global__ void __launch_bounds__(256, std::is_same<R, float>::value ? 2 : 1)
           }
           c[v][b] = s;
         }
-      const R fx = A.fxv[gi * NQ + qa];
+      const R fx = sfxv[tx * NQ + qa];
       R Pq[NV][NQ], Qq[NV][NQ];
 #pragma unroll
       for (int v = 0; v < NV; ++v)
@@ -461,7 +513,7 @@ __global__ void __launch_bounds__(256, std::is_same<R, float>::value ? 2 : 1)
           for (int b = 0; b < NQ; ++b) s += c[v][b] * T.B[b][qb];
           d[v] = s;
         }
-        eq_point(A, fx, A.fyv[gj * NQ + qb], re, pe);
+        eq_point(A, fx, sfyv[ty * NQ + qb], re, pe);
         if (A.compute_speed) {
           R ww = R(0.25) * T.wq[qa] * T.wq[qb];
           rbar += re * ww;
@@ -589,13 +641,57 @@ __global__ void __launch_bounds__(256, std::is_same<R, float>::value ? 2 : 1)
     }
   }
   if (A.compute_speed) {
-    double mx = block_max(spx, red);
-    double my = block_max(spy, red);
+    double mx = block_max(spx, red, tid, nthr);
+    double my = block_max(spy, red, tid, nthr);
     if (tid == 0) {
       atomicMax(&A.dev->smax[A.parity ^ 1][0], (unsigned long long)__double_as_longlong(mx));
       atomicMax(&A.dev->smax[A.parity ^ 1][1], (unsigned long long)__double_as_longlong(my));
     }
   }
+  __syncthreads();
+}
+
+// Persistent stage kernel: CTAs stride over the tiles of the grid; the next-but-one
+// tile is staged by cp.async while the current one is computed (double buffering).
+// The tile shape is a compile-time parameter so all shared-memory indexing folds.
+template <typename R, int K, int BASIS, int TX, int TY>
+__global__ void __launch_bounds__(TX *TY, std::is_same<R, float>::value ? 2 : 1)
+    k_stage(const __grid_constant__ StageArgs<R> A) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int tid = threadIdx.x;
+  const bool lim = A.limiter && A.lim_y && K >= 1;
+  const TileLayout L = tile_layout(K, BASIS, TX, TY, lim);
+  double *red = reinterpret_cast<double *>(smem_raw);
+  R *bufs = reinterpret_cast<R *>(smem_raw + 64 * sizeof(double));
+  R *flux = bufs + 2 * L.buf;
+  const int ntx = (A.nx + TX - 1) / TX, nty = (A.ny + TY - 1) / TY, ntiles = ntx * nty;
+  const double dt = stage_dt(A);
+  if (A.advance_time && blockIdx.x == 0 && tid == 0) {
+    DevState *S = A.dev;
+    S->t[A.parity ^ 1] = S->t[A.parity] + dt;
+    S->nstep[A.parity ^ 1] = S->nstep[A.parity] + (dt > 0.0 ? 1 : 0);
+    S->smax[A.parity ^ 1][0] = 0ull;
+    S->smax[A.parity ^ 1][1] = 0ull;
+  }
+  int t = blockIdx.x;
+  if (t < ntiles) tile_load_async<R, K, BASIS, TX, TY>(A, lim, (t % ntx) * TX, (t / ntx) * TY, bufs, tid);
+  cp_async_commit();
+  if (t + (int)gridDim.x < ntiles) {
+    const int t1 = t + gridDim.x;
+    tile_load_async<R, K, BASIS, TX, TY>(A, lim, (t1 % ntx) * TX, (t1 / ntx) * TY, bufs + L.buf, tid);
+  }
+  cp_async_commit();
+  for (int k = 0; t < ntiles; t += gridDim.x, ++k) {
+    cp_async_wait<1>();
+    __syncthreads();
+    R *buf = bufs + (k & 1) * L.buf;
+    tile_compute<R, K, BASIS, TX, TY>(A, lim, (t % ntx) * TX, (t / ntx) * TY, buf, flux, red, tid, dt);
+    const int tn = t + 2 * (int)gridDim.x;
+    if (tn < ntiles)
+      tile_load_async<R, K, BASIS, TX, TY>(A, lim, (tn % ntx) * TX, (tn / ntx) * TY, buf, tid);
+    cp_async_commit();
+  }
+  cp_async_wait<0>();
 }
 
 }  // namespace wb

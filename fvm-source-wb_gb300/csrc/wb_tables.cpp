@@ -45,10 +45,10 @@ void gauss_legendre(int n, double *x, double *w) {
     double phi[8], dphi[8];
     legendre_scaled(z, n, phi, dphi);
     double d = dphi[n] / std::sqrt(2.0 * n + 1.0);
-    x[n - 1 - i] = -z;  // ascending order
-    w[n - 1 - i] = 2.0 / ((1.0 - z * z) * d * d);
+    x[i] = -z;  // z runs from the largest root down, so x ascends
+    w[i] = 2.0 / ((1.0 - z * z) * d * d);
   }
-  // exact symmetry
+  // exact symmetry (x ascending: x[i] < 0 < x[n-1-i])
   for (int i = 0; i < n / 2; ++i) {
     double xm = 0.5 * (x[n - 1 - i] - x[i]), wm = 0.5 * (w[i] + w[n - 1 - i]);
     x[i] = -xm;

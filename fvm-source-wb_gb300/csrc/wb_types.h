@@ -100,6 +100,45 @@ struct StageArgs {
   DevState *dev;
 };
 
+// Layout of one staged tile in shared memory (offsets in elements):
+//   su  [NV*NB][RY][RX]  modes of the tile and a one-cell halo
+//   sm  [NV][LY][LX]     means of the tile and a two-cell halo (limiter only)
+//   eq  fxv[NQ*TX], fxf[TX+1], fyv[NQ*TY], fyf[TY+1]  equilibrium factors
+struct TileLayout {
+  int TX, TY, RX, RY, RXY, LX, LY, NB, NQ, lim;
+  int su, sm, eq, buf;
+};
+__host__ __device__ inline TileLayout tile_layout(int K, int basis, int TX, int TY, int lim) {
+  TileLayout L;
+  L.TX = TX;
+  L.TY = TY;
+  L.RX = TX + 2;
+  L.RY = TY + 2;
+  L.RXY = L.RX * L.RY;
+  L.LX = TX + 4;
+  L.LY = TY + 4;
+  L.NB = num_modes(K, basis);
+  L.NQ = K + 1;
+  L.lim = lim;
+  L.su = 0;
+  L.sm = NV * L.NB * L.RXY;
+  L.eq = L.sm + (lim ? NV * L.LY * L.LX : 0);
+  const int neq = L.NQ * TX + TX + 1 + L.NQ * TY + TY + 1;
+  L.buf = (L.eq + neq + 3) & ~3;  // 16-byte aligned double buffers
+  return L;
+}
+// Largest tile width the staging code handles (three 32-wide chunks of a halo row).
+constexpr int TILE_X_MAX = 92;
+
+// Shared-memory bytes of the stage kernel for a TX x TY tile: reduction scratch, two
+// staged tiles, and the x/y face fluxes of one tile.
+template <typename R>
+__host__ __device__ inline size_t stage_smem_bytes(int K, int basis, int TX, int TY, int lim) {
+  const TileLayout L = tile_layout(K, basis, TX, TY, lim);
+  const size_t flux = (size_t)NV * (K + 1) * ((size_t)TY * (TX + 1) + (size_t)(TY + 1) * TX);
+  return 64 * sizeof(double) + (2 * (size_t)L.buf + flux) * sizeof(R);
+}
+
 // Arguments of the per-cell auxiliary kernels (FP64 equilibrium factors).
 struct AuxArgs {
   int nx, ny;

@@ -140,6 +140,9 @@ int wb_evolve(wb_ctx *ctx, double tend, int32_t max_steps, int32_t *steps_done, 
 /* Waits for the context stream; reports a device-side non-physical flag. */
 int wb_sync(wb_ctx *ctx);
 int wb_get_time(wb_ctx *ctx, double *t, int64_t *steps);
+/* Sets the simulated time and step counter (checkpoint restart; the reference keeps t
+ * in evolve's locals and has no restart). */
+int wb_set_time(wb_ctx *ctx, double t, int64_t steps);
 
 /* The context's CUDA stream (a cudaStream_t), for callers that order their own work
  * against it or time it with CUDA events.  No counterpart in the reference (serial). */
@@ -157,6 +160,11 @@ int wb_stage_stats(wb_ctx *ctx, double *total_ms, int64_t *launches);
 int wb_norms(wb_ctx *ctx, wb_ctx *other, double l1[4], double linf[4], double l2[4]);
 /* FP64 domain integrals of the full conserved state (equilibrium + perturbation). */
 int wb_conserved_sums(wb_ctx *ctx, double sums[4]);
+/* Text snapshot in the reference's format: output_file, 2d/benchmark_2d_dg.f90:468-495 --
+ * one line per cell (x index outer, y inner) with x, y of the cell's first Gauss point
+ * and the primitive perturbation w - w_eq there for variables var..4, each written as
+ * Fortran 1PE12.5 followed by one blank. */
+int wb_write_dat(wb_ctx *ctx, const char *path, int32_t var);
 
 /* --- batched form -------------------------------------------------------------- */
 typedef struct wb_batch wb_batch;

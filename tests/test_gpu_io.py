@@ -1,0 +1,59 @@
+"""Checkpoint/restart and the reference's text snapshot format, on the GPU."""
+import numpy as np
+import pytest
+
+from helpers import base_cfg, orc_cfg, random_delta, solver
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("limiter", [0, 1])
+def test_restart_is_bitwise(wb, tmp_path, precision, limiter):
+    c = base_cfg(nx=20, ny=16, order=2, basis=1, limiter=limiter, bc_x=0)
+    # rough data only with the limiter on (unlimited P2 steps of rough data go non-physical)
+    d = random_delta(c, amp=3e-2 if limiter else 5e-3, seed=4, smooth=not limiter)
+    with solver(wb, c, precision) as a:
+        a.upload(d)
+        a.step(10)
+        ref = a.download()
+        tref, nref = a.time()
+    with solver(wb, c, precision) as b:
+        b.upload(d)
+        b.step(5)
+        b.save_checkpoint(str(tmp_path / "ck.bin"))
+    r = wb.Solver.from_checkpoint(str(tmp_path / "ck.bin"))
+    r.step(5)
+    got = r.download()
+    t, n = r.time()
+    r.close()
+    assert n == nref and t == tref
+    np.testing.assert_array_equal(got, ref)
+
+
+def test_output_file_format(wb, orc, tmp_path):
+    c = base_cfg(nx=6, ny=5, order=1, basis=0, eq_kind=1)
+    d = random_delta(c, amp=1e-2, seed=8)
+    with solver(wb, c, 0) as s:
+        s.upload(d)
+        s.output_file(str(tmp_path / "snap.dat"), var=1)
+        dl = s.download()
+    lines = open(tmp_path / "snap.dat").read().splitlines()
+    assert len(lines) == 30
+    for ln in lines:
+        assert len(ln) == 6 * 13  # six values of 12 columns, each followed by a blank
+    oc = orc_cfg(c)
+    nodes = orc.nodes_from_modes(oc, dl)
+    x, _ = orc.gl(2)
+    k = 0
+    for i in range(6):          # x index outer, y index inner, as output_file loops
+        for j in range(5):
+            vals = [float(v) for v in lines[k].split()]
+            xq = (i + 0.5) / 6 + 0.5 / 6 * x[0]
+            yq = (j + 0.5) / 5 + 0.5 / 5 * x[0]
+            re, pe = orc.eq_at(oc, xq, yq)
+            u = nodes[:, 0, j, i] + np.array([re, 0, 0, pe / 0.4])
+            w = [u[0] - re, u[1] / u[0], u[2] / u[0],
+                 0.4 * (u[3] - 0.5 * (u[1] ** 2 + u[2] ** 2) / u[0]) - pe]
+            np.testing.assert_allclose(vals, [xq, yq] + w, rtol=1e-5, atol=1e-16)
+            k += 1
