@@ -17,7 +17,7 @@ FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", 
 SOURCES = ["wb_stage_f32_k2p.cu", "wb_stage_f32_k2q.cu", "wb_stage_f64_k2p.cu",
            "wb_stage_f64_k2q.cu", "wb_kernels_f64.cu", "wb_kernels_f32.cu", "wb_stage_f32_k1p.cu",
            "wb_stage_f32_k1q.cu", "wb_stage_f64_k1p.cu", "wb_stage_f64_k1q.cu", "wb_stage_f32_k0.cu",
-           "wb_stage_f64_k0.cu", "wb_capi.cu", "wb_batch.cu", "wb_fv1d.cu", "wb_tables.cpp"]
+           "wb_stage_f64_k0.cu", "wb_capi.cu", "wb_batch.cu", "wb_fv1d.cu", "wb_noalloc.cu", "wb_tables.cpp"]
 
 
 def _deps():

@@ -160,6 +160,25 @@ int wb_stage_stats(wb_ctx *ctx, double *total_ms, int64_t *launches);
 int wb_norms(wb_ctx *ctx, wb_ctx *other, double l1[4], double linf[4], double l2[4]);
 /* FP64 domain integrals of the full conserved state (equilibrium + perturbation). */
 int wb_conserved_sums(wb_ctx *ctx, double sums[4]);
+
+/* Error norms (L1, Linf, L2 per conserved variable, as wb_norms) of two device-resident
+ * FP64 modal states a and b (SoA, plane_stride elements between (variable, mode) planes;
+ * b may be NULL for the norms of a) that allocates no device memory.  No counterpart in
+ * the reference.  It is for callers that cannot call cudaMalloc where they need the norms:
+ * a host whose device memory is all owned by its own pool or by another runtime, or a time
+ * loop that must not take the device-wide synchronisation cudaMalloc/cudaFree imply.
+ * Its reduction scratch is a fixed array inside the library, 1.5 MB on every device that
+ * loads the library and held until the process exits, so grids are limited to
+ * WB_NORMS_NOALLOC_MAX_CELLS cells; a larger grid returns WB_ERR_ARG (use wb_norms).  The
+ * first call on a device sets that device up (looks up the array's device address and
+ * uploads the basis tables): make the first call before any stream capture.  Every call
+ * uses the same array, so calls that overlap on the GPU (other streams, other threads)
+ * race.  stream may be NULL (the default stream); the call waits for it before it returns
+ * the host results. */
+#define WB_NORMS_NOALLOC_MAX_CELLS 4194304
+int wb_norms_device_noalloc(int32_t nx, int32_t ny, int32_t order, int32_t basis, double lx,
+                            double ly, const double *a, const double *b, size_t plane_stride,
+                            void *stream, double l1[4], double linf[4], double l2[4]);
 /* Text snapshot in the reference's format: output_file, 2d/benchmark_2d_dg.f90:468-495 --
  * one line per cell (x index outer, y inner) with x, y of the cell's first Gauss point
  * and the primitive perturbation w - w_eq there for variables var..4, each written as

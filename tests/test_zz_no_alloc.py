@@ -1,0 +1,68 @@
+"""The allocation-free norm entry point, called through the C ABI and checked against the
+context's own norms (wb_norms).
+
+Callers whose device memory is all owned by their own pool or by another runtime, or
+whose time loop must not take the device-wide synchronisation of cudaMalloc/cudaFree,
+cannot allocate where they need error norms; wb_norms_device_noalloc serves them from a
+fixed scratch array inside the library.  This file is collected last, so a run that stops
+at the first failure has already run every other test.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from helpers import base_cfg, random_delta, solver
+
+pytestmark = pytest.mark.gpu
+
+
+def _entry(wb):
+    f = wb.lib().wb_norms_device_noalloc
+    f.argtypes = ([ctypes.c_int32] * 4 + [ctypes.c_double] * 2 + [ctypes.c_void_p] * 2 +
+                  [ctypes.c_size_t, ctypes.c_void_p] + [ctypes.c_void_p] * 3)
+    f.restype = ctypes.c_int32
+    return f
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def test_noalloc_norms_match_context_norms(wb):
+    f = _entry(wb)
+    c = base_cfg(nx=40, ny=24, order=2, basis=1, limiter=0, bc_x=0)
+    with solver(wb, c, 0) as a, solver(wb, c, 0) as b:
+        a.upload(random_delta(c, seed=31))
+        b.upload(random_delta(c, seed=32))
+        r1, rinf, r2 = a.compute_error(b)       # the context path (its own scratch)
+        s1, sinf, s2 = a.compute_error(None)
+        pa, plane = a.device_state()
+        pb, _ = b.device_state()
+        for _ in range(2):  # consecutive calls reuse the same fixed scratch
+            l1, linf, l2 = np.zeros(4), np.zeros(4), np.zeros(4)
+            rc = f(c["nx"], c["ny"], c["order"], c["basis"], c["lx"], c["ly"], pa, pb, plane,
+                   None, _ptr(l1), _ptr(linf), _ptr(l2))
+            assert rc == wb.WB_OK
+            np.testing.assert_allclose(l1, r1, rtol=1e-13)
+            np.testing.assert_allclose(linf, rinf, rtol=1e-13)
+            np.testing.assert_allclose(l2, r2, rtol=1e-13)
+            # b = NULL gives the norms of a alone
+            rc = f(c["nx"], c["ny"], c["order"], c["basis"], c["lx"], c["ly"], pa, None, plane,
+                   None, _ptr(l1), _ptr(linf), _ptr(l2))
+            assert rc == wb.WB_OK
+            np.testing.assert_allclose(l1, s1, rtol=1e-13)
+            np.testing.assert_allclose(linf, sinf, rtol=1e-13)
+            np.testing.assert_allclose(l2, s2, rtol=1e-13)
+
+
+def test_noalloc_rejects_grids_beyond_its_scratch(wb):
+    f = _entry(wb)
+    c = base_cfg(nx=8, ny=8, order=1, basis=1)
+    with solver(wb, c, 0) as a:
+        pa, plane = a.device_state()
+        l1, linf, l2 = np.zeros(4), np.zeros(4), np.zeros(4)
+        # 4096 x 2048 cells exceed WB_NORMS_NOALLOC_MAX_CELLS: rejected before any launch
+        rc = f(4096, 2048, 1, 1, 1.0, 1.0, pa, None, 4096 * 2048, None, _ptr(l1), _ptr(linf),
+               _ptr(l2))
+        assert rc == wb.WB_ERR_ARG
