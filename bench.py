@@ -217,11 +217,18 @@ def run_ours(args):
     dev = lr
     torch.cuda.set_device(dev)
     name = args.workload
-    w32 = wb.workload(name, wb.PREC_FP32)
+    size = {} if args.nx <= 0 else {"nx": args.nx, "ny": args.nx}
+    fixed = {}
+    if args.tile:
+        tx, ty = (int(v) for v in args.tile.lower().split("x"))
+        fixed = {"tile_x": tx, "tile_y": ty}
+    w32 = wb.workload(name, wb.PREC_FP32, **size, **fixed)
     ic = wb.workload_ic(name)
     s32 = wb.Solver(device=dev, **w32)
     dof = s32.dofs
     s32.init_perturbation(ic)
+    # fastest compiled tile shape for this grid (state preserved), unless one is given
+    tile = (fixed["tile_x"], fixed["tile_y"]) if fixed else s32.autotune(2)
     s32.step(args.warmup)
     s32.sync()
     stream = torch.cuda.ExternalStream(s32.stream(), device=dev)
@@ -262,7 +269,7 @@ def run_ours(args):
     extra = {}
     if rank == 0 and not args.quick:
         # FP64 plain on the same grid
-        w64 = wb.workload(name, wb.PREC_FP64)
+        w64 = wb.workload(name, wb.PREC_FP64, **size)
         s64 = wb.Solver(device=dev, **w64)
         s64.init_perturbation(ic)
         s64.step(1)
@@ -326,10 +333,11 @@ def run_ours(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded 16-mode velocity field on the isothermal atmosphere)",
-            "config": {"workload": "cfg5: 8192^2 P2 isothermal Phi=0.1y, 16-mode velocity field, "
-                                   "FP32-perturbation, SSP-RK2, CFL 0.3",
+            "config": {"workload": "cfg5: %d^2 P2 isothermal Phi=0.1y, 16-mode velocity field, "
+                                   "FP32-perturbation, SSP-RK2, CFL 0.3" % w32["nx"],
                        "nx": w32["nx"], "ny": w32["ny"], "order": 2, "basis": "P",
-                       "dofs": dof, "parallelism": "replicas" if world > 1 else "single",
+                       "dofs": dof, "tile": list(tile),
+                       "parallelism": "replicas" if world > 1 else "single",
                        "l2_policy": "inputs larger than L2 (6.4 GB state per buffer)"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "clocks": clocks,
@@ -354,6 +362,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-n", type=int, default=512)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--nx", type=int, default=0,
+                    help="cells per side instead of the workload's (small cases for profiling)")
+    ap.add_argument("--tile", default="", help="fixed stage tile TXxTY (default: autotune)")
     ap.add_argument("--quick", action="store_true", help="skip FP64, accuracy and CPU legs")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -25,6 +25,7 @@ EQ_NONE, EQ_ISOTHERMAL, EQ_POLYTROPE = 0, 1, 2
 LLF_MAXABS, LLF_REF2D = 0, 1
 PREC_FP64, PREC_FP32 = 0, 1
 RK2, RK54 = 0, 1
+LIMITER_NONE, LIMITER_MINMOD, LIMITER_POSITIVITY = 0, 1, 2
 LAYOUT_SOA, LAYOUT_FORTRAN = 0, 1
 
 
@@ -40,7 +41,7 @@ class WbConfig(ctypes.Structure):
         "precision", "integrator", "tile_x", "tile_y", "device")] + [
         (n, ctypes.c_double) for n in (
             "gamma", "gx", "gy", "rho0", "p0", "kpoly", "lx", "ly", "lim_norm", "lim_M",
-            "lim_tol", "cfl")]
+            "lim_tol", "cfl", "pos_eps")]
 
 
 class WbPerturbation(ctypes.Structure):
@@ -74,6 +75,7 @@ def lib():
             "wb_num_modes": ([i32, i32], i32), "wb_mode_list": ([i32, i32, p, p], i32),
             "wb_upload_state": ([p, p, i32], i32), "wb_download_state": ([p, p, i32], i32),
             "wb_upload_state_f32": ([p, p], i32), "wb_download_state_f32": ([p, p], i32),
+            "wb_download_state_raw": ([p, p], i32),
             "wb_init_perturbation": ([p, p], i32), "wb_device_state": ([p, p, p], i32),
             "wb_compute_update": ([p, p, p, i32], i32), "wb_apply_limiter": ([p], i32),
             "wb_max_speed": ([p, p, p], i32), "wb_step": ([p, i32, d], i32),
@@ -82,6 +84,7 @@ def lib():
             "wb_norms": ([p, p, p, p, p], i32), "wb_write_dat": ([p, ctypes.c_char_p, i32], i32),
             "wb_conserved_sums": ([p, p], i32), "wb_get_stream": ([p, p], i32),
             "wb_profile_stages": ([p, i32], i32), "wb_stage_stats": ([p, p, p], i32),
+            "wb_autotune": ([p, i32, p, p], i32),
             "wb_batch_create": ([p, i32, p], i32), "wb_batch_destroy": ([p], i32),
             "wb_batch_last_error": ([p], ctypes.c_char_p),
             "wb_batch_init_perturbation": ([p, p], i32), "wb_batch_step": ([p, i32, d], i32),
@@ -286,6 +289,12 @@ class Solver:
         self._check(lib().wb_download_state(self._ctx, _ptr(out), layout))
         return out
 
+    def download_raw(self):
+        """The resident state as stored (before the limit-on-load), in the context's precision."""
+        out = np.zeros(self.shape, dtype=self.dtype)
+        self._check(lib().wb_download_state_raw(self._ctx, _ptr(out)))
+        return out
+
     def upload_f32(self, delta):
         a = np.ascontiguousarray(delta, dtype=np.float32).reshape(self.shape)
         self._check(lib().wb_upload_state_f32(self._ctx, _ptr(a)))
@@ -348,10 +357,10 @@ class Solver:
     _MAGIC = b"WBGB300\x00"
 
     def save_checkpoint(self, path):
-        """Writes config, t, step count and the (limited) state; a restart from it
-        continues bitwise identically (the limiter is idempotent on its own output)."""
+        """Writes config, t, step count and the resident state as stored (before the
+        limit-on-load); a restart from it continues bit for bit."""
         t, n = self.time()
-        state = self.download_f32() if self.dtype == np.float32 else self.download()
+        state = self.download_raw()
         hdr = {"config": {k: getattr(self.cfg, k) for k, _ in WbConfig._fields_},
                "t": t, "steps": n, "dtype": str(state.dtype), "shape": list(state.shape)}
         h = json.dumps(hdr).encode()
@@ -411,6 +420,13 @@ class Solver:
         p = ctypes.c_void_p()
         self._check(lib().wb_get_stream(self._ctx, ctypes.byref(p)))
         return p.value or 0
+
+    def autotune(self, steps=3):
+        """Pick the fastest compiled tile shape for this grid (state is preserved)."""
+        tx = ctypes.c_int32()
+        ty = ctypes.c_int32()
+        self._check(lib().wb_autotune(self._ctx, int(steps), ctypes.byref(tx), ctypes.byref(ty)))
+        return tx.value, ty.value
 
     def profile_stages(self, on=True):
         self._check(lib().wb_profile_stages(self._ctx, 1 if on else 0))

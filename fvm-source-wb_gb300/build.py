@@ -4,6 +4,7 @@
 """
 import concurrent.futures as cf
 import os
+import re
 import subprocess
 import sys
 
@@ -14,10 +15,34 @@ LIB = os.path.join(OUT, "libwbgb300.so")
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
-SOURCES = ["wb_stage_f32_k2p.cu", "wb_stage_f32_k2q.cu", "wb_stage_f64_k2p.cu",
-           "wb_stage_f64_k2q.cu", "wb_kernels_f64.cu", "wb_kernels_f32.cu", "wb_stage_f32_k1p.cu",
-           "wb_stage_f32_k1q.cu", "wb_stage_f64_k1p.cu", "wb_stage_f64_k1q.cu", "wb_stage_f32_k0.cu",
-           "wb_stage_f64_k0.cu", "wb_capi.cu", "wb_batch.cu", "wb_fv1d.cu", "wb_noalloc.cu", "wb_tables.cpp"]
+SOURCES = ["wb_kernels_f64.cu", "wb_kernels_f32.cu", "wb_capi.cu", "wb_batch.cu", "wb_fv1d.cu",
+           "wb_noalloc.cu", "wb_stage_dispatch.cu", "wb_tables.cpp"]
+GEN = os.path.join(OUT, "gen")
+
+
+def stage_instances():
+    """The lines of csrc/wb_stage_instances.h: (P, R, K, BT, B, TX, TY, POS)."""
+    txt = open(os.path.join(CSRC, "wb_stage_instances.h")).read()
+    pat = r"X\((\w+), (\w+), (\d), (\w), (\d), (\d+), (\d+), (\d)\)"
+    return re.findall(pat, txt)
+
+
+def generate_stage_units():
+    """One translation unit per compiled stage kernel (so nvcc runs them in parallel)."""
+    os.makedirs(GEN, exist_ok=True)
+    names = []
+    for inst in stage_instances():
+        P, R, K, BT, B, TX, TY, POS = inst
+        name = "stage_%s_k%s%s_%sx%s_%s.cu" % (P, K, BT, TX, TY, POS)
+        body = ('// generated by build.py from wb_stage_instances.h\n'
+                '#include "wb_stage_launch.cuh"\n'
+                'WB_STAGE_INSTANCE(%s)\n' % ", ".join(inst))
+        path = os.path.join(GEN, name)
+        if not os.path.exists(path) or open(path).read() != body:
+            with open(path, "w") as f:
+                f.write(body)
+        names.append(path)
+    return names
 
 
 def _deps():
@@ -34,11 +59,11 @@ def _stale(obj, src, deps):
 
 
 def _compile(src, force):
-    s = os.path.join(CSRC, src)
-    o = os.path.join(OUT, src.rsplit(".", 1)[0] + ".o")
+    s = src if os.path.isabs(src) else os.path.join(CSRC, src)
+    o = os.path.join(OUT, os.path.basename(src).rsplit(".", 1)[0] + ".o")
     if not force and not _stale(o, s, _deps()):
         return o, None
-    cmd = [NVCC] + ARCH + FLAGS + ["-c", s, "-o", o]
+    cmd = [NVCC] + ARCH + FLAGS + ["-I", CSRC, "-c", s, "-o", o]
     if src.endswith(".cpp"):
         cmd = [NVCC] + FLAGS + ["-x", "c++", "-c", s, "-o", o]
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -49,8 +74,11 @@ def _compile(src, force):
 
 def build(force=False, verbose=False):
     os.makedirs(OUT, exist_ok=True)
-    srcs = [s for s in SOURCES if os.path.exists(os.path.join(CSRC, s))]
-    with cf.ThreadPoolExecutor(max_workers=len(srcs)) as ex:
+    # slowest units first: the generated stage kernels, then the rest
+    srcs = generate_stage_units() + SOURCES
+    srcs.sort(key=lambda p: 0 if "_k2" in p else 1)
+    jobs = max(2, min(len(srcs), os.cpu_count() or 8))
+    with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
         results = list(ex.map(lambda s: _compile(s, force), srcs))
     errs = [e for _, e in results if e]
     if errs:

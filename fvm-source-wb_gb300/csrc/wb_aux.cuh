@@ -32,6 +32,23 @@ __global__ void k_limit(const __grid_constant__ StageArgs<R> A, R *u) {
   if (gi >= A.nx || gj >= A.ny || K < 1) return;
   const long long P = A.plane, nx = A.nx;
   const long long cell = gj * nx + gi;
+  if (A.limiter == 2) {
+    constexpr int NQ = K + 1;
+    R fx[NQ], fy[NQ];
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      fx[q] = A.fxv[gi * NQ + q];
+      fy[q] = A.fyv[gj * NQ + q];
+    }
+    R dl[NV * NB];
+#pragma unroll
+    for (int k = 0; k < NV * NB; ++k) dl[k] = u[(long long)k * P + cell];
+    positivity_cell<R, K, BASIS>(A, dl, fx, fy);
+#pragma unroll
+    for (int k = 1; k < NV * NB; ++k)
+      if (k % NB) u[(long long)k * P + cell] = dl[k];
+    return;
+  }
   int iw = wrap_index(gi - 1, A.nx, A.bc_x), ie = wrap_index(gi + 1, A.nx, A.bc_x);
   int js = wrap_index(gj - 1, A.ny, A.bc_y), jn = wrap_index(gj + 1, A.ny, A.bc_y);
 #pragma unroll

@@ -27,6 +27,7 @@ struct wb_batch {
   int nitems = 0;
   size_t smem = 0;
   int bufsz = 0;
+  int pos = 0;                        // some instance runs the positivity limiter
   StageArgs<float> *args = nullptr;  // [6 phases][2 stages][n]
   const float **state_ptrs = nullptr;  // [6 phases][n] current state per phase
   int phase = 0;
@@ -78,8 +79,8 @@ int build_args(wb_batch *b, int dt_mode, double dt) {
 int launch_phase(wb_batch *b, int p) {
   const int n = (int)b->inst.size();
   int grid = 0;
-  BCK(launch_batch_stage(b->args + ((size_t)p * 2 + 0) * n, b->items, b->nitems, b->bufsz, b->smem, &grid, b->stream));
-  BCK(launch_batch_stage(b->args + ((size_t)p * 2 + 1) * n, b->items, b->nitems, b->bufsz, b->smem, &grid, b->stream));
+  BCK(launch_batch_stage(b->args + ((size_t)p * 2 + 0) * n, b->items, b->nitems, b->bufsz, b->smem, b->pos, &grid, b->stream));
+  BCK(launch_batch_stage(b->args + ((size_t)p * 2 + 1) * n, b->items, b->nitems, b->bufsz, b->smem, b->pos, &grid, b->stream));
   return WB_OK;
 }
 
@@ -156,7 +157,8 @@ int wb_batch_create(const wb_config *cfgs, int32_t n, wb_batch **out) {
     for (int j0 = 0; j0 < c.ny; j0 += ty)
       for (int i0 = 0; i0 < c.nx; i0 += tx)
         items.push_back(make_int4(i, i0, j0, (c.order << 24) | (tx << 12) | ty));
-    const TileLayout L = tile_layout(c.order, WB_BASIS_P, tx, ty, c.limiter && c.order >= 1);
+    const TileLayout L = tile_layout(c.order, WB_BASIS_P, tx, ty, c.limiter == 1 && c.order >= 1);
+    if (c.limiter == 2 && c.order >= 1) b->pos = 1;
     bufmax = std::max(bufmax, L.buf);
     fluxmax = std::max(fluxmax, (size_t)NV * (c.order + 1) * ((size_t)ty * (tx + 1) + (size_t)(ty + 1) * tx));
   }

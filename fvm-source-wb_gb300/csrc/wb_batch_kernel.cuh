@@ -28,7 +28,7 @@ __device__ __forceinline__ void item_load(const StageArgs<R> *__restrict__ args,
   int K, TX, TY;
   unpack_item(w, K, TX, TY);
   const StageArgs<R> &A = args[w.x];
-  const bool lim = A.limiter && A.lim_y && K >= 1;
+  const bool lim = A.limiter == 1 && A.lim_y && K >= 1;
   if (K == 0) tile_load_async<R, 0, 1, BATCH_TX, BATCH_TY>(A, lim, w.y, w.z, buf, tid);
   else if (K == 1) tile_load_async<R, 1, 1, BATCH_TX, BATCH_TY>(A, lim, w.y, w.z, buf, tid);
   else tile_load_async<R, 2, 1, BATCH_TX, BATCH_TY>(A, lim, w.y, w.z, buf, tid);
@@ -36,7 +36,7 @@ __device__ __forceinline__ void item_load(const StageArgs<R> *__restrict__ args,
 
 // Persistent batched stage: CTAs stride over the work list; the next-but-one item is
 // staged (cp.async) while the current one is computed.  bufsz = the largest tile buffer.
-template <typename R>
+template <typename R, bool POS>
 __global__ void __launch_bounds__(256, 2)
     k_batch_stage(const StageArgs<R> *__restrict__ args, const int4 *__restrict__ items, int nitems,
                   int bufsz) {
@@ -67,10 +67,10 @@ __global__ void __launch_bounds__(256, 2)
       S->smax[A.parity ^ 1][0] = 0ull;
       S->smax[A.parity ^ 1][1] = 0ull;
     }
-    const bool lim = A.limiter && A.lim_y && K >= 1;
-    if (K == 0) tile_compute<R, 0, 1, BATCH_TX, BATCH_TY>(A, lim, w.y, w.z, buf, flux, red, tid, dt);
-    else if (K == 1) tile_compute<R, 1, 1, BATCH_TX, BATCH_TY>(A, lim, w.y, w.z, buf, flux, red, tid, dt);
-    else tile_compute<R, 2, 1, BATCH_TX, BATCH_TY>(A, lim, w.y, w.z, buf, flux, red, tid, dt);
+    const bool lim = A.limiter == 1 && A.lim_y && K >= 1;
+    if (K == 0) tile_compute<R, 0, 1, BATCH_TX, BATCH_TY, POS>(A, lim, w.y, w.z, buf, flux, red, tid, dt);
+    else if (K == 1) tile_compute<R, 1, 1, BATCH_TX, BATCH_TY, POS>(A, lim, w.y, w.z, buf, flux, red, tid, dt);
+    else tile_compute<R, 2, 1, BATCH_TX, BATCH_TY, POS>(A, lim, w.y, w.z, buf, flux, red, tid, dt);
     const int in = it + 2 * (int)gridDim.x;
     if (in < nitems) item_load(args, items[in], sA[k & 1], buf, tid, nthr);
     cp_async_commit();

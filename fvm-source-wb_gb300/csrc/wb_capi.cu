@@ -2,6 +2,7 @@
 // well-balanced step: context lifetime, state transfer, the stage loop of evolve, and
 // diagnostics.  Kernels live in the per-precision translation units.
 #include <cuda_runtime.h>
+#include <dlfcn.h>
 
 #include <cmath>
 #include <cstdio>
@@ -76,7 +77,9 @@ int validate(const wb_config *c, std::string &why) {
     double phimax = std::fmax(0.0, c->gx * c->lx) + std::fmax(0.0, c->gy * c->ly);
     if (!(1.0 - k * phimax > 0.0)) return why = "polytrope density vanishes inside the domain", WB_ERR_CONFIG;
   }
-  if (c->limiter && !(c->lim_norm > 0.0)) return why = "lim_norm must be > 0", WB_ERR_CONFIG;
+  if (c->limiter < 0 || c->limiter > 2) return why = "bad limiter (0 off, 1 minmod, 2 positivity)", WB_ERR_CONFIG;
+  if (c->limiter == 1 && !(c->lim_norm > 0.0)) return why = "lim_norm must be > 0", WB_ERR_CONFIG;
+  if (c->limiter == 2 && !(c->pos_eps > 0.0)) return why = "pos_eps must be > 0", WB_ERR_CONFIG;
   if (c->tile_x < 0 || c->tile_y < 0) return why = "bad tile", WB_ERR_CONFIG;
   if (c->tile_x > 0 || c->tile_y > 0) {
     long long t = (long long)c->tile_x * c->tile_y;
@@ -112,6 +115,8 @@ StageArgs<R> base_args(const wb_ctx *c) {
   A.hgam = (R)(g.gamma / (g.gamma - 1.0));
   A.gx = (R)g.gx;
   A.gy = (R)g.gy;
+  A.gx4 = (R)(0.25 * g.gx);
+  A.gy4 = (R)(0.25 * g.gy);
   A.rho0 = (R)g.rho0;
   A.p0 = (R)g.p0;
   A.kpoly = (R)g.kpoly;
@@ -120,6 +125,7 @@ StageArgs<R> base_args(const wb_ctx *c) {
   A.lim_Mdx2 = (R)(g.lim_M * dx * dx);
   A.lim_Mdy2 = (R)(g.lim_M * dy * dy);
   A.lim_tol = (R)g.lim_tol;
+  A.pos_eps = (R)g.pos_eps;
   A.fxv = (const R *)c->fxv;
   A.fxf = (const R *)c->fxf;
   A.fyv = (const R *)c->fyv;
@@ -427,6 +433,40 @@ int dev_to_host(wb_ctx *ctx, const void *src, int layout, double *h) {
   return WB_OK;
 }
 
+// ---- tile cache: lines "precision order basis nx ny tile_x tile_y" (last match wins)
+std::string tile_cache_path() {
+  const char *e = std::getenv("WB_TILE_CACHE");
+  if (e && *e) return e;
+  Dl_info info;
+  if (dladdr((void *)&wb_create, &info) && info.dli_fname) {
+    std::string f = info.dli_fname;
+    size_t slash = f.find_last_of('/');
+    return (slash == std::string::npos ? std::string(".") : f.substr(0, slash)) + "/tile_cache.txt";
+  }
+  return "tile_cache.txt";
+}
+bool tile_cache_lookup(const wb_config &c, int *tx, int *ty) {
+  FILE *f = std::fopen(tile_cache_path().c_str(), "r");
+  if (!f) return false;
+  int p, o, b, nx, ny, x, y;
+  bool found = false;
+  while (std::fscanf(f, "%d %d %d %d %d %d %d", &p, &o, &b, &nx, &ny, &x, &y) == 7)
+    if (p == c.precision && o == c.order && b == c.basis && nx == c.nx && ny == c.ny &&
+        tile_supported(p == WB_PREC_FP32, x, y)) {
+      *tx = x;
+      *ty = y;
+      found = true;
+    }
+  std::fclose(f);
+  return found;
+}
+void tile_cache_store(const wb_config &c, int tx, int ty) {
+  FILE *f = std::fopen(tile_cache_path().c_str(), "a");
+  if (!f) return;
+  std::fprintf(f, "%d %d %d %d %d %d %d\n", c.precision, c.order, c.basis, c.nx, c.ny, tx, ty);
+  std::fclose(f);
+}
+
 }  // namespace
 
 extern "C" {
@@ -468,6 +508,7 @@ int wb_config_default(wb_config *c) {
   c->lim_M = 0.0;       // M = 0, 2d/parameters_dg_2d.f90:38
   c->lim_tol = 1e-6;    // 2d/limiters.f90:262
   c->cfl = 0.2;         // 2d/parameters_dg_2d.f90:26
+  c->pos_eps = 1e-10;   // eps, 2d/parameters_dg_2d.f90:28
   return WB_OK;
 }
 
@@ -552,6 +593,7 @@ int wb_create(const wb_config *cfg, wb_ctx **out) {
     ctx->TX = 16;
     ctx->TY = 8;
   }
+  if (cfg->tile_x <= 0) tile_cache_lookup(*cfg, &ctx->TX, &ctx->TY);
   // basis tables (constant memory of both precisions' kernels, FP64 copy in global)
   Tab1D<double> t64[KMAX + 1];
   Tab1D<float> t32[KMAX + 1];
@@ -620,6 +662,17 @@ int wb_download_state(wb_ctx *ctx, double *delta, int32_t layout) {
     if ((rc = limited_copy<double>(ctx, &d))) return rc;
     if ((rc = dev_to_host(ctx, d, layout, delta))) return rc;
   }
+  return check_dev_err(ctx);
+}
+
+int wb_download_state_raw(wb_ctx *ctx, void *delta) {
+  if (!ctx || !delta) return WB_ERR_ARG;
+  CK(cudaSetDevice(ctx->cfg.device));
+  const size_t es = is_fp32(ctx) ? sizeof(float) : sizeof(double);
+  const size_t rowb = (size_t)ctx->ncell * es;
+  CK(cudaMemcpy2DAsync(delta, rowb, state_buf(ctx, 0), ctx->plane * es, rowb, NV * ctx->nb,
+                       cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
   return check_dev_err(ctx);
 }
 
@@ -784,6 +837,66 @@ int wb_step(wb_ctx *ctx, int32_t nsteps, double dt) {
   if (!ctx || nsteps < 0) return WB_ERR_ARG;
   CK(cudaSetDevice(ctx->cfg.device));
   return step_impl(ctx, nsteps, dt > 0.0 ? 0 : 1, dt, -1.0);
+}
+
+int wb_autotune(wb_ctx *ctx, int32_t steps, int32_t *tile_x, int32_t *tile_y) {
+  if (!ctx || steps < 1) return WB_ERR_ARG;
+  CK(cudaSetDevice(ctx->cfg.device));
+  const int fp32 = is_fp32(ctx);
+  const int cand[2][2] = {{32, 8}, {16, 16}};
+  const int ncand = fp32 ? 2 : 1;
+  const int c64[1][2] = {{16, 8}};
+  // save the run so every candidate starts from the same state
+  void *backup = nullptr;
+  int rc = dalloc(ctx, (char **)&backup, ctx->state_bytes);
+  if (rc) return rc;
+  DevState saved;
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpy(backup, state_buf(ctx, 0), ctx->state_bytes, cudaMemcpyDeviceToDevice));
+  CK(cudaMemcpy(&saved, ctx->dev, sizeof(saved), cudaMemcpyDeviceToHost));
+  const int cur0 = ctx->cur, par0 = ctx->parity;
+  const bool sv0 = ctx->speed_valid;
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  float best = 0.0f;
+  int bx = ctx->TX, by = ctx->TY;
+  for (int k = 0; k < ncand && rc == WB_OK; ++k) {
+    ctx->cur = cur0;
+    ctx->parity = par0;
+    ctx->speed_valid = sv0;
+    CK(cudaMemcpy(state_buf(ctx, 0), backup, ctx->state_bytes, cudaMemcpyDeviceToDevice));
+    CK(cudaMemcpy(ctx->dev, &saved, sizeof(saved), cudaMemcpyHostToDevice));
+    ctx->TX = fp32 ? cand[k][0] : c64[k][0];
+    ctx->TY = fp32 ? cand[k][1] : c64[k][1];
+    if ((rc = step_impl(ctx, 1, 1, 0.0, -1.0))) break;  // warm-up (first launch set-up)
+    CK(cudaEventRecord(e0, ctx->stream));
+    if ((rc = step_impl(ctx, steps, 1, 0.0, -1.0))) break;
+    CK(cudaEventRecord(e1, ctx->stream));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.0f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    if (k == 0 || ms < best) {
+      best = ms;
+      bx = ctx->TX;
+      by = ctx->TY;
+    }
+  }
+  ctx->cur = cur0;
+  ctx->parity = par0;
+  ctx->speed_valid = sv0;
+  cudaMemcpy(state_buf(ctx, 0), backup, ctx->state_bytes, cudaMemcpyDeviceToDevice);
+  cudaMemcpy(ctx->dev, &saved, sizeof(saved), cudaMemcpyHostToDevice);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(backup);
+  if (rc) return rc;
+  ctx->TX = bx;
+  ctx->TY = by;
+  tile_cache_store(ctx->cfg, bx, by);
+  if (tile_x) *tile_x = bx;
+  if (tile_y) *tile_y = by;
+  return WB_OK;
 }
 
 int wb_sync(wb_ctx *ctx) {

@@ -22,55 +22,20 @@ namespace wb {
 WB_DECLARE_PRECISION_ENTRY_POINTS(float)
 WB_DECLARE_PRECISION_ENTRY_POINTS(double)
 
-// stage translation units (one per precision, degree and basis)
-#define WB_DECLARE_STAGE_TU(R, TAG)                                                             \
-  cudaError_t upload_tables_##TAG(const Tab1D<R> *t);                                          \
-  cudaError_t launch_stage_##TAG(const StageArgs<R> &A, int TX, int TY, cudaStream_t s);
-WB_DECLARE_STAGE_TU(float, f32_k0)
-WB_DECLARE_STAGE_TU(float, f32_k1q)
-WB_DECLARE_STAGE_TU(float, f32_k1p)
-WB_DECLARE_STAGE_TU(float, f32_k2q)
-WB_DECLARE_STAGE_TU(float, f32_k2p)
-WB_DECLARE_STAGE_TU(double, f64_k0)
-WB_DECLARE_STAGE_TU(double, f64_k1q)
-WB_DECLARE_STAGE_TU(double, f64_k1p)
-WB_DECLARE_STAGE_TU(double, f64_k2q)
-WB_DECLARE_STAGE_TU(double, f64_k2p)
-
-inline cudaError_t launch_stage(const StageArgs<float> &A, int K, int basis, int TX, int TY,
-                                cudaStream_t s) {
-  if (K == 0) return launch_stage_f32_k0(A, TX, TY, s);
-  if (K == 1) return basis == 0 ? launch_stage_f32_k1q(A, TX, TY, s) : launch_stage_f32_k1p(A, TX, TY, s);
-  return basis == 0 ? launch_stage_f32_k2q(A, TX, TY, s) : launch_stage_f32_k2p(A, TX, TY, s);
-}
-inline cudaError_t launch_stage(const StageArgs<double> &A, int K, int basis, int TX, int TY,
-                                cudaStream_t s) {
-  if (K == 0) return launch_stage_f64_k0(A, TX, TY, s);
-  if (K == 1) return basis == 0 ? launch_stage_f64_k1q(A, TX, TY, s) : launch_stage_f64_k1p(A, TX, TY, s);
-  return basis == 0 ? launch_stage_f64_k2q(A, TX, TY, s) : launch_stage_f64_k2p(A, TX, TY, s);
-}
-// Uploads the basis tables to the constant memory of every translation unit.
-inline cudaError_t upload_tables(const Tab1D<float> *t32, const Tab1D<double> *t64) {
-  cudaError_t (*f32[])(const Tab1D<float> *) = {upload_tables_aux, upload_tables_f32_k0,
-                                                upload_tables_f32_k1q, upload_tables_f32_k1p,
-                                                upload_tables_f32_k2q, upload_tables_f32_k2p};
-  cudaError_t (*f64[])(const Tab1D<double> *) = {upload_tables_aux, upload_tables_f64_k0,
-                                                 upload_tables_f64_k1q, upload_tables_f64_k1p,
-                                                 upload_tables_f64_k2q, upload_tables_f64_k2p};
-  for (auto f : f32) {
-    cudaError_t e = f(t32);
-    if (e != cudaSuccess) return e;
-  }
-  for (auto f : f64) {
-    cudaError_t e = f(t64);
-    if (e != cudaSuccess) return e;
-  }
-  return cudaSuccess;
-}
+// Stage kernels (wb_stage_dispatch.cu): the compiled kernel for precision, degree K,
+// basis and tile TX x TY (and the positivity limiter when the launch needs it).
+cudaError_t launch_stage(const StageArgs<float> &A, int K, int basis, int TX, int TY,
+                         cudaStream_t s);
+cudaError_t launch_stage(const StageArgs<double> &A, int K, int basis, int TX, int TY,
+                         cudaStream_t s);
 // Tile shapes the stage kernels are compiled for.
-inline bool tile_supported(int precision_fp32, int tx, int ty) {
-  if (precision_fp32) return (tx == 32 && ty == 8) || (tx == 16 && ty == 16);
-  return tx == 16 && ty == 8;
+bool tile_supported(int precision_fp32, int tx, int ty);
+
+// Constant-memory basis tables of the auxiliary kernels, both precisions.
+inline cudaError_t upload_tables(const Tab1D<float> *t32, const Tab1D<double> *t64) {
+  cudaError_t e = upload_tables_aux(t32);
+  if (e != cudaSuccess) return e;
+  return upload_tables_aux(t64);
 }
 
 // FP64-only diagnostics and precision conversion (defined in wb_kernels_f64.cu)
@@ -82,7 +47,7 @@ cudaError_t launch_f64_to_f32(float *out, const double *in, long long n, cudaStr
 
 // batched form (FP32): persistent stage over a work list; per-instance max speed
 cudaError_t launch_batch_stage(const StageArgs<float> *args, const int4 *items, int nitems,
-                               int bufsz, size_t smem, int *grid_out, cudaStream_t s);
+                               int bufsz, size_t smem, int pos, int *grid_out, cudaStream_t s);
 cudaError_t launch_batch_max_speed(const StageArgs<float> *args, const float *const *state,
                                    const int4 *items, int nitems, cudaStream_t s);
 

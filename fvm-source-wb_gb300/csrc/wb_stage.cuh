@@ -3,9 +3,10 @@
 // One CTA owns a TX x TY tile of cells.  Per stage it
 //   1. stages the perturbation modes of the tile plus a one-cell halo in shared memory
 //      (and, when the limiter is on, the cell means of a two-cell halo);
-//   2. applies the minmod moment limiter to every staged cell (limit-on-load: stage
-//      outputs are stored unlimited and every consumer limits what it reads, which is
-//      the same as the reference's apply_limiter after each stage);
+//   2. applies the limiter to every staged cell -- the minmod moment limiter or the
+//      Zhang-Shu positivity limiter (limit-on-load: stage outputs are stored unlimited
+//      and every consumer limits what it reads, which is the same as the reference's
+//      apply_limiter after each stage);
 //   3. computes every x- and y-face flux of the tile once (LLF on equilibrium face
 //      state + perturbation traces, minus the equilibrium flux);
 //   4. per cell: volume and source quadrature of the split fluxes, edge integrals,
@@ -25,9 +26,24 @@
 //   __constant__ wb::Tab1D<R> c_tab[KMAX+1];
 #pragma once
 #include <type_traits>
+#include "wb_ctab.h"
 #include "wb_types.h"
 
 namespace wb {
+
+// Compile-time basis tables of degree K in the kernel's precision.
+template <typename R, int K>
+struct TC {
+  static __device__ __forceinline__ constexpr R B(int a, int q) { return R(CTab<K>::B(a, q)); }
+  static __device__ __forceinline__ constexpr R D(int a, int q) { return R(CTab<K>::D(a, q)); }
+  static __device__ __forceinline__ constexpr R BW(int a, int q) { return R(CTab<K>::BW(a, q)); }
+  static __device__ __forceinline__ constexpr R DW(int a, int q) { return R(CTab<K>::DW(a, q)); }
+  static __device__ __forceinline__ constexpr R Ep(int a) { return R(CTab<K>::Ep(a)); }
+  static __device__ __forceinline__ constexpr R Em(int a) { return R(CTab<K>::Em(a)); }
+  static __device__ __forceinline__ constexpr R wq(int q) { return R(CTab<K>::wq(q)); }
+  static constexpr int NG = CTab<K>::NG;
+  static __device__ __forceinline__ constexpr R Gl(int a, int g) { return R(CTab<K>::Gl(a, g)); }
+};
 
 __device__ __forceinline__ int wrap_index(int i, int n, int bc) {
   if (i >= 0 && i < n) return i;
@@ -103,7 +119,7 @@ __device__ __forceinline__ void flux_lit(const double *u, const double *w, doubl
   }
 }
 
-// Volume point: split fluxes and source, already scaled by 0.5/dx, 0.5/dy, 0.25.
+// Volume point: split fluxes (unscaled) and source (scaled by the 0.25 of the assembly).
 template <typename R>
 __device__ __forceinline__ void vol_point(const StageArgs<R> &A, const R *d, R re, R pe, R *Fx,
                                           R *Fy, R *S) {
@@ -116,11 +132,11 @@ __device__ __forceinline__ void vol_point(const StageArgs<R> &A, const R *d, R r
     flux_lit<0>(u, w, f);
     flux_lit<0>(ue, we, fe);
 #pragma unroll
-    for (int v = 0; v < NV; ++v) Fx[v] = (f[v] - fe[v]) * A.hidx;
+    for (int v = 0; v < NV; ++v) Fx[v] = f[v] - fe[v];
     flux_lit<1>(u, w, f);
     flux_lit<1>(ue, we, fe);
 #pragma unroll
-    for (int v = 0; v < NV; ++v) Fy[v] = (f[v] - fe[v]) * A.hidy;
+    for (int v = 0; v < NV; ++v) Fy[v] = f[v] - fe[v];
     // rounded products (never contracted into the subtraction below): S(u_eq + 0) and
     // S(u_eq) must round identically so a zero perturbation cancels exactly
     double s[NV], se[NV];
@@ -144,18 +160,18 @@ __device__ __forceinline__ void vol_point(const StageArgs<R> &A, const R *d, R r
     R vx = d[1] * inv, vy = d[2] * inv;
     R dp = A.gm1 * (d[3] - R(0.5) * (d[1] * vx + d[2] * vy));
     R H = A.hgam * pe + d[3] + dp;
-    Fx[0] = d[1] * A.hidx;
-    Fx[1] = (d[1] * vx + dp) * A.hidx;
-    Fx[2] = (d[2] * vx) * A.hidx;
-    Fx[3] = (vx * H) * A.hidx;
-    Fy[0] = d[2] * A.hidy;
-    Fy[1] = (d[1] * vy) * A.hidy;
-    Fy[2] = (d[2] * vy + dp) * A.hidy;
-    Fy[3] = (vy * H) * A.hidy;
+    Fx[0] = d[1];
+    Fx[1] = d[1] * vx + dp;
+    Fx[2] = d[2] * vx;
+    Fx[3] = vx * H;
+    Fy[0] = d[2];
+    Fy[1] = d[1] * vy;
+    Fy[2] = d[2] * vy + dp;
+    Fy[3] = vy * H;
     S[0] = R(0);
-    S[1] = -(d[0] * A.gx) * R(0.25);
-    S[2] = -(d[0] * A.gy) * R(0.25);
-    S[3] = -(d[1] * A.gx + d[2] * A.gy) * R(0.25);
+    S[1] = -(d[0] * A.gx4);
+    S[2] = -(d[0] * A.gy4);
+    S[3] = -(d[1] * A.gx4 + d[2] * A.gy4);
   }
 }
 
@@ -235,6 +251,119 @@ __device__ __forceinline__ void limit_modes(const StageArgs<R> &A, R *base, int 
   }
 }
 
+// Zhang-Shu positivity limiter on one cell, compute_positivity (2d/limiters.f90:478-654),
+// in delta form: the limiter acts on the full-state polynomial W = e + d, e the cell's
+// projected equilibrium (density and energy modes; zero momentum), and writes back
+// d' = s W - e = s d + (s - 1) e for the non-mean modes, s = theta t for the density and
+// t for the other variables.  The positivity set is compute_set's (2d/limiters.f90:438-475):
+// Gauss-Lobatto nodes in one direction times Gauss nodes in the other, both ways.
+// d[v*NB + m] holds the cell's modes (updated in place); fx / fy are the cell's NQ
+// equilibrium factors at the volume points.  A cell the limiter leaves alone
+// (theta = t = 1) is not written.  Not inlined: it is off the default path, and its
+// point loops stay rolled to keep the stage kernels small.
+template <typename R, int K, int BASIS>
+__device__ __noinline__ void positivity_cell(const StageArgs<R> &A, R *d, const R *fx,
+                                             const R *fy) {
+  if constexpr (K >= 1) {
+    constexpr int NB = num_modes(K, BASIS), NQ = K + 1;
+    using T = TC<R, K>;
+    constexpr int NG = T::NG;
+    R er[NB], ee[NB];
+#pragma unroll
+    for (int m = 0; m < NB; ++m) er[m] = ee[m] = R(0);
+#pragma unroll 1
+    for (int qa = 0; qa < NQ; ++qa)
+#pragma unroll 1
+      for (int qb = 0; qb < NQ; ++qb) {
+        R re, pe;
+        eq_point(A, fx[qa], fy[qb], re, pe);
+        pe *= A.igm1;
+        const R w = R(0.25) * T::wq(qa) * T::wq(qb);
+#pragma unroll
+        for (int m = 0; m < NB; ++m) {
+          const int a = mode_deg(K, BASIS, m, 0), b = mode_deg(K, BASIS, m, 1);
+          const R bw = w * (T::B(a, qa) * T::B(b, qb));
+          er[m] += re * bw;
+          ee[m] += pe * bw;
+        }
+      }
+    R W[NV][NB];
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+#pragma unroll
+      for (int m = 0; m < NB; ++m) {
+        const R x = d[v * NB + m];
+        W[v][m] = v == 0 ? er[m] + x : (v == 3 ? ee[m] + x : x);
+      }
+    const R eps = A.pos_eps;
+    // density: theta = min(|(rho_avg - eps) / (rho_avg - rho_min)|, 1)
+    const R rbar = W[0][0];
+    R rmin = rbar;
+#pragma unroll 1
+    for (int p = 0; p < 2 * NQ * NG; ++p) {
+      const int fam = p / (NQ * NG), q = (p / NG) % NQ, g = p % NG;
+      R r = R(0);
+#pragma unroll
+      for (int m = 0; m < NB; ++m) {
+        const int a = mode_deg(K, BASIS, m, 0), b = mode_deg(K, BASIS, m, 1);
+        r += W[0][m] * (fam == 0 ? T::Gl(a, g) * T::B(b, q) : T::B(a, q) * T::Gl(b, g));
+      }
+      rmin = fmin(rmin, r);
+    }
+    const R theta = fmin(fabs((rbar - eps) / (rbar - rmin)), R(1));
+    // pressure on the density-limited set; solve_for_t (2d/limiters.f90:312-362) where
+    // p <= eps
+    R tmin = R(1);
+#pragma unroll 1
+    for (int p = 0; p < 2 * NQ * NG; ++p) {
+      const int fam = p / (NQ * NG), q = (p / NG) % NQ, g = p % NG;
+      R u[NV];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        R sacc = R(0);
+#pragma unroll
+        for (int m = 1; m < NB; ++m) {
+          const int a = mode_deg(K, BASIS, m, 0), b = mode_deg(K, BASIS, m, 1);
+          sacc += W[v][m] * (fam == 0 ? T::Gl(a, g) * T::B(b, q) : T::B(a, q) * T::Gl(b, g));
+        }
+        u[v] = W[v][0] + (v == 0 ? theta * sacc : sacc);
+      }
+      const R rf = rfmax(u[0], R(1.0e-9f));
+      const R pr = A.gm1 * (u[3] - R(0.5) * (u[1] * u[1] + u[2] * u[2]) / rf);
+      if (!(pr > eps)) {
+        const R dr = u[0] - W[0][0], dmx = u[1] - W[1][0], dmy = u[2] - W[2][0];
+        const R de = u[3] - W[3][0];
+        const R qa = R(2) * dr * de - dmx * dmx - dmy * dmy;
+        R qb = R(2) * dr * (W[3][0] - eps * A.igm1) + R(2) * W[0][0] * de -
+               R(2) * (W[1][0] * dmx + W[2][0] * dmy);
+        R qc = R(2) * W[0][0] * W[3][0] - (W[1][0] * W[1][0] + W[2][0] * W[2][0]) -
+               R(2) * eps * W[0][0] * A.igm1;
+        qb = qb / qa;
+        qc = qc / qa;
+        const R D = sqrt(fabs(qb * qb - R(4) * qc));
+        const R t1 = R(0.5) * (-qb - D), t2 = R(0.5) * (-qb + D);
+        R t;
+        if (t1 > -eps && t1 < R(1) + eps) t = t1;
+        else if (t2 > -eps && t2 < R(1) + eps) t = t2;
+        else t = R(0);
+        t = fmax(R(0), fmin(R(1), t));
+        if (tmin >= t) tmin = t;
+      }
+    }
+    if (theta < R(1) || tmin < R(1)) {
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        const R sc = v == 0 ? theta * tmin : tmin;
+#pragma unroll
+        for (int m = 1; m < NB; ++m) {
+          const R e = v == 0 ? er[m] : (v == 3 ? ee[m] : R(0));
+          d[v * NB + m] = sc * d[v * NB + m] + (sc - R(1)) * e;
+        }
+      }
+    }
+  }
+}
+
 __device__ __forceinline__ double block_max(double v, double *red, int tid, int nthr) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
@@ -288,47 +417,82 @@ __device__ __forceinline__ void tile_load_async(const StageArgs<R> &A, const boo
   const int lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
   const int nx = A.nx, ny = A.ny;
   const long long P = A.plane;
-  int gc[3];
-#pragma unroll
-  for (int k = 0; k < 3; ++k) gc[k] = wrap_index(i0 + lane + 32 * k - 1, nx, A.bc_x);
+  constexpr int PX = TX + 8;
+  constexpr int VEC = 16 / (int)sizeof(R);  // elements per 16-byte chunk
+  constexpr int CPR = PX / VEC;             // chunks per stored row
+  // x-interior tile with 16-byte aligned rows: copy [i0-4, i0+TX+4) of every row in
+  // 16-byte chunks (rows still BC-mapped in y); otherwise element-wise with x mapping
+  const bool vec = i0 >= 4 && i0 + TX + 4 <= nx && (nx % VEC) == 0;
   const int nrow = NV * L.NB * L.RY;
-  for (int row = warp; row < nrow; row += nwarp) {
-    const int pl = row / L.RY, ry = row - pl * L.RY;
-    const int gj = wrap_index(j0 + ry - 1, ny, A.bc_y);
-    const R *src = A.x + pl * P + (long long)gj * nx;
-    R *dst = buf + L.su + row * L.RX;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const int c = lane + 32 * k;
-      if (c < L.RX) cp_async<sizeof(R)>(dst + c, src + gc[k]);
+  if (vec) {
+    for (int k = tid; k < nrow * CPR; k += nthr) {
+      const int row = k / CPR, ch = k - row * CPR;
+      const int pl = row / L.RY, ry = row - pl * L.RY;
+      const int gj = wrap_index(j0 + ry - 1, ny, A.bc_y);
+      cp_async<16>(buf + L.su + row * PX + ch * VEC,
+                   A.x + pl * P + (long long)gj * nx + (i0 - 4) + ch * VEC);
     }
-  }
-  if (L.lim) {
+  } else {
+    int gc[3];
 #pragma unroll
-    for (int k = 0; k < 3; ++k) gc[k] = wrap_index(i0 + lane + 32 * k - 2, nx, A.bc_x);
-    const int mrow = NV * L.LY;
-    for (int row = warp; row < mrow; row += nwarp) {
-      const int v = row / L.LY, ly = row - v * L.LY;
-      const int gj = wrap_index(j0 + ly - 2, ny, A.bc_y);
-      const R *src = A.x + (long long)(v * L.NB) * P + (long long)gj * nx;
-      R *dst = buf + L.sm + row * L.LX;
+    for (int k = 0; k < 3; ++k) gc[k] = wrap_index(i0 + lane + 32 * k - 1, nx, A.bc_x);
+    for (int row = warp; row < nrow; row += nwarp) {
+      const int pl = row / L.RY, ry = row - pl * L.RY;
+      const int gj = wrap_index(j0 + ry - 1, ny, A.bc_y);
+      const R *src = A.x + pl * P + (long long)gj * nx;
+      R *dst = buf + L.su + row * PX + 3;
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
         const int c = lane + 32 * k;
-        if (c < L.LX) cp_async<sizeof(R)>(dst + c, src + gc[k]);
+        if (c < L.RX) cp_async<sizeof(R)>(dst + c, src + gc[k]);
       }
     }
   }
-  // equilibrium factors: fxv [NQ*TX], fxf [TX+1], fyv [NQ*TY], fyf [TY+1] (indices clamped)
-  const int NQ = L.NQ;
-  const int n1 = NQ * TX, n2 = n1 + TX + 1, n3 = n2 + NQ * TY, n4 = n3 + TY + 1;
+  if (L.lim) {
+    const int mrow = NV * L.LY;
+    if (vec) {
+      for (int k = tid; k < mrow * CPR; k += nthr) {
+        const int row = k / CPR, ch = k - row * CPR;
+        const int v = row / L.LY, ly = row - v * L.LY;
+        const int gj = wrap_index(j0 + ly - 2, ny, A.bc_y);
+        cp_async<16>(buf + L.sm + row * PX + ch * VEC,
+                     A.x + (long long)(v * L.NB) * P + (long long)gj * nx + (i0 - 4) + ch * VEC);
+      }
+    } else {
+      int gc[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) gc[k] = wrap_index(i0 + lane + 32 * k - 2, nx, A.bc_x);
+      for (int row = warp; row < mrow; row += nwarp) {
+        const int v = row / L.LY, ly = row - v * L.LY;
+        const int gj = wrap_index(j0 + ly - 2, ny, A.bc_y);
+        const R *src = A.x + (long long)(v * L.NB) * P + (long long)gj * nx;
+        R *dst = buf + L.sm + row * PX + 2;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const int c = lane + 32 * k;
+          if (c < L.LX) cp_async<sizeof(R)>(dst + c, src + gc[k]);
+        }
+      }
+    }
+  }
+  // equilibrium factors: fxv [NQ*(TX+2)] and fyv [NQ*(TY+2)] of the tile and its halo
+  // (BC-mapped like the modes), fxf [TX+1] and fyf [TY+1] (indices clamped)
+  constexpr int NQ = K + 1;
+  constexpr int n1 = NQ * (TX + 2), n2 = n1 + TX + 1, n3 = n2 + NQ * (TY + 2), n4 = n3 + TY + 1;
   R *e = buf + L.eq;
   for (int k = tid; k < n4; k += nthr) {
     const R *src;
-    if (k < n1) src = A.fxv + min(i0 * NQ + k, nx * NQ - 1);
-    else if (k < n2) src = A.fxf + min(i0 + (k - n1), nx);
-    else if (k < n3) src = A.fyv + min(j0 * NQ + (k - n2), ny * NQ - 1);
-    else src = A.fyf + min(j0 + (k - n3), ny);
+    if (k < n1) {
+      const int c = k / NQ, q = k - c * NQ;
+      src = A.fxv + wrap_index(i0 - 1 + c, nx, A.bc_x) * NQ + q;
+    } else if (k < n2) {
+      src = A.fxf + min(i0 + (k - n1), nx);
+    } else if (k < n3) {
+      const int r = (k - n2) / NQ, q = (k - n2) - r * NQ;
+      src = A.fyv + wrap_index(j0 - 1 + r, ny, A.bc_y) * NQ + q;
+    } else {
+      src = A.fyf + min(j0 + (k - n3), ny);
+    }
     cp_async<sizeof(R)>(e + k, src);
   }
 }
@@ -336,27 +500,30 @@ __device__ __forceinline__ void tile_load_async(const StageArgs<R> &A, const boo
 // Compute one staged tile: limiter, face fluxes, cell quadrature, RK combination and the
 // wave-speed reduction.  Thread tid owns cell (tid % TX, tid / TX).  Ends with a CTA
 // barrier, after which `buf` and the flux area may be reused.
-template <typename R, int K, int BASIS, int TX, int TY>
+template <typename R, int K, int BASIS, int TX, int TY, bool POS>
 __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool lim_,
                                              const int i0, const int j0, R *buf, R *flux,
                                              double *red, const int tid, const double dt) {
   constexpr int NQ = K + 1;
   constexpr int NB = num_modes(K, BASIS);
-  const Tab1D<R> &T = c_tab[K];
+  using T = TC<R, K>;
   const TileLayout L = tile_layout(K, BASIS, TX, TY, lim_);
-  const int RX = L.RX, RY = L.RY, RXY = L.RXY;
-  const int LX = L.LX, LY = L.LY;
+  // RX / LX below are the stored row pitch (TX + 8); the staged ring starts at column 3
+  // (modes) and 2 (means) of each stored row
+  constexpr int RX = TX + 8, RY = TY + 2, RXY = RX * RY, RXL = TX + 2;
+  constexpr int LX = TX + 8, LY = TY + 4;
   constexpr int nthr = TX * TY;
   const int nx = A.nx, ny = A.ny;
   const long long P = A.plane;
   const bool lim = lim_;
-  (void)RY;
-  R *su = buf + L.su;
-  R *sm = buf + L.sm;
-  const R *sfxv = buf + L.eq;
-  const R *sfxf = sfxv + NQ * TX;
-  const R *sfyv = sfxf + TX + 1;
-  const R *sfyf = sfyv + NQ * TY;
+  R *su = buf + L.su + 3;
+  R *sm = buf + L.sm + 2;
+  // volume-point factors are indexed from the tile's first column / row (halo at -1)
+  const R *sfxv = buf + L.eq + NQ;
+  const R *sfxf = buf + L.eq + NQ * (TX + 2);
+  const R *sfyv = sfxf + TX + 1 + NQ;
+  const R *sfyf = sfxf + TX + 1 + NQ * (TY + 2);
+  const bool pos = POS && A.limiter == 2 && A.lim_y && K >= 1;
   R *sfx = flux;
   const int FXS = TY * (TX + 1);
   R *sfy = sfx + NV * NQ * FXS;
@@ -364,12 +531,24 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
 
   // 2. limiter on every staged cell (means never change, so cells are independent)
   if (lim) {
-    for (int e = tid; e < NV * RXY; e += nthr) {
-      int rx = e % RX, t1 = e / RX, ry = t1 % RY, v = t1 / RY;
+    for (int e = tid; e < NV * RY * RXL; e += nthr) {
+      int rx = e % RXL, t1 = e / RXL, ry = t1 % RY, v = t1 / RY;
       const R *mv = sm + v * LY * LX;
       int c = (ry + 1) * LX + (rx + 1);
       limit_modes<R, K, BASIS>(A, su + (v * NB) * RXY + ry * RX + rx, RXY, mv[c], mv[c - 1],
                                mv[c + 1], mv[c - LX], mv[c + LX]);
+    }
+    __syncthreads();
+  } else if (pos) {
+    for (int e = tid; e < RY * RXL; e += nthr) {
+      const int rx = e % RXL, ry = e / RXL;
+      R *base = su + ry * RX + rx;
+      R dl[NV * NB];
+#pragma unroll
+      for (int k = 0; k < NV * NB; ++k) dl[k] = base[k * RXY];
+      positivity_cell<R, K, BASIS>(A, dl, sfxv + (rx - 1) * NQ, sfyv + (ry - 1) * NQ);
+#pragma unroll
+      for (int k = 0; k < NV * NB; ++k) base[k * RXY] = dl[k];
     }
     __syncthreads();
   }
@@ -396,13 +575,14 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
           int m = mode_index(K, BASIS, a, b);
           if (m < 0) continue;
           const R *pm = su + (v * NB + m) * RXY + (fj + 1) * RX;
-          sl += pm[fi] * T.Ep[a];
-          sr += pm[fi + 1] * T.Em[a];
+          sl += pm[fi] * T::Ep(a);
+          sr += pm[fi + 1] * T::Em(a);
         }
         cl[v][b] = sl;
         cr[v][b] = sr;
       }
     const R fxf = sfxf[fi];
+    R mom[NV][NQ];
 #pragma unroll
     for (int q = 0; q < NQ; ++q) {
       R dL[NV], dR[NV], F[NV], re, pe;
@@ -411,8 +591,8 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
         R sl = R(0), sr = R(0);
 #pragma unroll
         for (int b = 0; b < NQ; ++b) {
-          sl += cl[v][b] * T.B[b][q];
-          sr += cr[v][b] * T.B[b][q];
+          sl += cl[v][b] * T::B(b, q);
+          sr += cr[v][b] * T::B(b, q);
         }
         dL[v] = sl;
         dR[v] = sr;
@@ -420,8 +600,15 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
       eq_point(A, fxf, sfyv[fj * NQ + q], re, pe);
       face_point<R, 0>(A, dL, dR, re, pe, F);
 #pragma unroll
-      for (int v = 0; v < NV; ++v) sfx[(v * NQ + q) * FXS + f] = F[v];
+      for (int v = 0; v < NV; ++v)
+#pragma unroll
+        for (int b = 0; b < NQ; ++b) mom[v][b] = (q == 0 ? R(0) : mom[v][b]) + F[v] * T::BW(b, q);
     }
+    // edge moments sum_q F(q) phi_b(eta_q) w_q, scaled by 0.5/dx, shared by both cells
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+#pragma unroll
+      for (int b = 0; b < NQ; ++b) sfx[(v * NQ + b) * FXS + f] = mom[v][b] * A.hidx;
     } else {
     const int f = fa - FXS;
     int fi = f % TX, fj = f / TX;
@@ -438,13 +625,14 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
           int m = mode_index(K, BASIS, a, b);
           if (m < 0) continue;
           const R *pm = su + (v * NB + m) * RXY + (fi + 1);
-          sb += pm[fj * RX] * T.Ep[b];
-          st += pm[(fj + 1) * RX] * T.Em[b];
+          sb += pm[fj * RX] * T::Ep(b);
+          st += pm[(fj + 1) * RX] * T::Em(b);
         }
         cb[v][a] = sb;
         ct[v][a] = st;
       }
     const R fyf = sfyf[fj];
+    R mom[NV][NQ];
 #pragma unroll
     for (int q = 0; q < NQ; ++q) {
       R dB[NV], dT[NV], F[NV], re, pe;
@@ -453,8 +641,8 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
         R sb = R(0), st = R(0);
 #pragma unroll
         for (int a = 0; a < NQ; ++a) {
-          sb += cb[v][a] * T.B[a][q];
-          st += ct[v][a] * T.B[a][q];
+          sb += cb[v][a] * T::B(a, q);
+          st += ct[v][a] * T::B(a, q);
         }
         dB[v] = sb;
         dT[v] = st;
@@ -462,8 +650,14 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
       eq_point(A, sfxv[fi * NQ + q], fyf, re, pe);
       face_point<R, 1>(A, dB, dT, re, pe, F);
 #pragma unroll
-      for (int v = 0; v < NV; ++v) sfy[(v * NQ + q) * FYS + f] = F[v];
+      for (int v = 0; v < NV; ++v)
+#pragma unroll
+        for (int a = 0; a < NQ; ++a) mom[v][a] = (q == 0 ? R(0) : mom[v][a]) + F[v] * T::BW(a, q);
     }
+#pragma unroll
+    for (int v = 0; v < NV; ++v)
+#pragma unroll
+      for (int a = 0; a < NQ; ++a) sfy[(v * NQ + a) * FYS + f] = mom[v][a] * A.hidy;
     }
   }
   __syncthreads();
@@ -493,7 +687,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
           for (int a = 0; a < NQ; ++a) {
             int m = mode_index(K, BASIS, a, b);
             if (m < 0) continue;
-            s += uc[(v * NB + m) * RXY] * T.B[a][qa];
+            s += uc[(v * NB + m) * RXY] * T::B(a, qa);
           }
           c[v][b] = s;
         }
@@ -510,25 +704,31 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
         for (int v = 0; v < NV; ++v) {
           R s = R(0);
 #pragma unroll
-          for (int b = 0; b < NQ; ++b) s += c[v][b] * T.B[b][qb];
+          for (int b = 0; b < NQ; ++b) s += c[v][b] * T::B(b, qb);
           d[v] = s;
         }
         eq_point(A, fx, sfyv[ty * NQ + qb], re, pe);
         if (A.compute_speed) {
-          R ww = R(0.25) * T.wq[qa] * T.wq[qb];
+          R ww = R(0.25) * T::wq(qa) * T::wq(qb);
           rbar += re * ww;
           pbar += pe * ww;
         }
         vol_point(A, d, re, pe, Fx, Fy, S);
+        // x fluxes are weighted by 0.5/dx once per qa below; y fluxes take 0.5/dy here
 #pragma unroll
-        for (int v = 0; v < NV; ++v)
+        for (int b = 0; b < NQ; ++b) {
+          const R dwy = b > 0 ? A.hidy * T::DW(b, qb) : R(0);
 #pragma unroll
-          for (int b = 0; b < NQ; ++b) {
-            Pq[v][b] += Fx[v] * T.BW[b][qb];
-            Qq[v][b] += S[v] * T.BW[b][qb];
-            if (b > 0) Qq[v][b] += Fy[v] * T.DW[b][qb];
+          for (int v = 0; v < NV; ++v) {
+            if (BASIS == 0 || b < K) Pq[v][b] += Fx[v] * T::BW(b, qb);
+            Qq[v][b] += S[v] * T::BW(b, qb);
+            if (b > 0) Qq[v][b] += Fy[v] * dwy;
           }
+        }
       }
+      R dwx[NQ];
+#pragma unroll
+      for (int a = 0; a < NQ; ++a) dwx[a] = A.hidx * T::DW(a, qa);
 #pragma unroll
       for (int v = 0; v < NV; ++v)
 #pragma unroll
@@ -536,38 +736,27 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
           constexpr int dummy = 0;
           (void)dummy;
           int a = mode_deg(K, BASIS, m, 0), b = mode_deg(K, BASIS, m, 1);
-          R t = T.BW[a][qa] * Qq[v][b];
-          if (a > 0) t += T.DW[a][qa] * Pq[v][b];
+          R t = T::BW(a, qa) * Qq[v][b];
+          if (a > 0) t += dwx[a] * Pq[v][b];
           acc[v][m] += t;
         }
     }
-    // edge integrals (faces of this cell from shared memory)
+    // edge integrals: the faces' moments (already weighted by 0.5/dx, 0.5/dy)
     const int fl = ty * (TX + 1) + tx, fb = ty * TX + tx;
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
       R FR[NQ], FL[NQ], GT[NQ], GB[NQ];
 #pragma unroll
       for (int b = 0; b < NQ; ++b) {
-        R r = R(0), l = R(0), t = R(0), bt = R(0);
-#pragma unroll
-        for (int q = 0; q < NQ; ++q) {
-          const R *px = sfx + (v * NQ + q) * FXS;
-          const R *py = sfy + (v * NQ + q) * FYS;
-          r += px[fl + 1] * T.BW[b][q];
-          l += px[fl] * T.BW[b][q];
-          t += py[fb + TX] * T.BW[b][q];
-          bt += py[fb] * T.BW[b][q];
-        }
-        FR[b] = r;
-        FL[b] = l;
-        GT[b] = t;
-        GB[b] = bt;
+        FR[b] = sfx[(v * NQ + b) * FXS + fl + 1];
+        FL[b] = sfx[(v * NQ + b) * FXS + fl];
+        GT[b] = sfy[(v * NQ + b) * FYS + fb + TX];
+        GB[b] = sfy[(v * NQ + b) * FYS + fb];
       }
 #pragma unroll
       for (int m = 0; m < NB; ++m) {
         int a = mode_deg(K, BASIS, m, 0), b = mode_deg(K, BASIS, m, 1);
-        acc[v][m] -= A.hidx * (T.Ep[a] * FR[b] - T.Em[a] * FL[b]) +
-                     A.hidy * (T.Ep[b] * GT[a] - T.Em[b] * GB[a]);
+        acc[v][m] -= (T::Ep(a) * FR[b] - T::Em(a) * FL[b]) + (T::Ep(b) * GT[a] - T::Em(b) * GB[a]);
       }
     }
 
@@ -592,7 +781,18 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
         for (int v = 0; v < NV; ++v)
 #pragma unroll
           for (int m = 0; m < NB; ++m) w[v][m] = in[(long long)(v * NB + m) * P + cell];
-        if (o.lim[ii] && A.limiter && K >= 1) {
+        if (POS && o.lim[ii] && A.limiter == 2 && K >= 1) {
+          R dl[NV * NB];
+#pragma unroll
+          for (int v = 0; v < NV; ++v)
+#pragma unroll
+            for (int m = 0; m < NB; ++m) dl[v * NB + m] = w[v][m];
+          positivity_cell<R, K, BASIS>(A, dl, sfxv + tx * NQ, sfyv + ty * NQ);
+#pragma unroll
+          for (int v = 0; v < NV; ++v)
+#pragma unroll
+            for (int m = 0; m < NB; ++m) w[v][m] = dl[v * NB + m];
+        } else if (o.lim[ii] && A.limiter == 1 && K >= 1) {
           int iw = wrap_index(gi - 1, nx, A.bc_x), ie = wrap_index(gi + 1, nx, A.bc_x);
           int js = wrap_index(gj - 1, ny, A.bc_y), jn = wrap_index(gj + 1, ny, A.bc_y);
 #pragma unroll
@@ -654,12 +854,14 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
 // Persistent stage kernel: CTAs stride over the tiles of the grid; the next-but-one
 // tile is staged by cp.async while the current one is computed (double buffering).
 // The tile shape is a compile-time parameter so all shared-memory indexing folds.
-template <typename R, int K, int BASIS, int TX, int TY>
+// POS compiles the positivity limiter in (limiter 2); without it the kernel carries no
+// positivity code at all.
+template <typename R, int K, int BASIS, int TX, int TY, bool POS>
 __global__ void __launch_bounds__(TX *TY, std::is_same<R, float>::value ? 2 : 1)
     k_stage(const __grid_constant__ StageArgs<R> A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int tid = threadIdx.x;
-  const bool lim = A.limiter && A.lim_y && K >= 1;
+  const bool lim = A.limiter == 1 && A.lim_y && K >= 1;  // minmod: stage the means halo
   const TileLayout L = tile_layout(K, BASIS, TX, TY, lim);
   double *red = reinterpret_cast<double *>(smem_raw);
   R *bufs = reinterpret_cast<R *>(smem_raw + 64 * sizeof(double));
@@ -685,7 +887,7 @@ __global__ void __launch_bounds__(TX *TY, std::is_same<R, float>::value ? 2 : 1)
     cp_async_wait<1>();
     __syncthreads();
     R *buf = bufs + (k & 1) * L.buf;
-    tile_compute<R, K, BASIS, TX, TY>(A, lim, (t % ntx) * TX, (t / ntx) * TY, buf, flux, red, tid, dt);
+    tile_compute<R, K, BASIS, TX, TY, POS>(A, lim, (t % ntx) * TX, (t / ntx) * TY, buf, flux, red, tid, dt);
     const int tn = t + 2 * (int)gridDim.x;
     if (tn < ntiles)
       tile_load_async<R, K, BASIS, TX, TY>(A, lim, (tn % ntx) * TX, (tn / ntx) * TY, buf, tid);

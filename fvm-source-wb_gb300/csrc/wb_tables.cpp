@@ -1,10 +1,13 @@
 // wb_tables.cpp -- host-side basis, quadrature and equilibrium tables.
 //
 // The basis is the scaled Legendre family phi_a = sqrt(2a+1) P_a of 2d/legendre.f90:1-50
-// (evaluated here by the Bonnet recurrence), the quadrature is (k+1)-point
-// Gauss-Legendre (2d/legendre.f90:77-108 computes it by Newton iteration; so does
-// this file, from the Chebyshev-node starting guess).
+// with (k+1)-point Gauss-Legendre quadrature (2d/legendre.f90:77-108 computes it by Newton
+// iteration).  The kernels' tables are the exact values of gen_ctab.py (wb_ctab.h);
+// gauss_legendre / legendre_scaled below evaluate the same family at run time (Newton from
+// the Chebyshev-node guess, Bonnet recurrence) for other uses.
 #include "wb_tables.h"
+
+#include "wb_ctab.h"
 
 #include <cmath>
 
@@ -58,33 +61,37 @@ void gauss_legendre(int n, double *x, double *w) {
   if (n % 2 == 1) x[n / 2] = 0.0;
 }
 
-void make_tab1d(Tab1D<double> tabs[KMAX + 1]) {
-  for (int k = 0; k <= KMAX; ++k) {
-    Tab1D<double> &t = tabs[k];
-    for (int a = 0; a < NQMAX; ++a) {
-      t.xq[a] = t.wq[a] = t.Ep[a] = t.Em[a] = 0.0;
-      for (int q = 0; q < NQMAX; ++q) t.B[a][q] = t.D[a][q] = t.BW[a][q] = t.DW[a][q] = 0.0;
-    }
-    const int nq = k + 1;
-    gauss_legendre(nq, t.xq, t.wq);
-    for (int q = 0; q < nq; ++q) {
-      double phi[8], dphi[8];
-      legendre_scaled(t.xq[q], k, phi, dphi);
-      for (int a = 0; a <= k; ++a) {
-        t.B[a][q] = phi[a];
-        t.D[a][q] = dphi[a];
-        t.BW[a][q] = phi[a] * t.wq[q];
-        t.DW[a][q] = dphi[a] * t.wq[q];
-      }
-    }
-    double pp[8], pm[8];
-    legendre_scaled(1.0, k, pp, nullptr);
-    legendre_scaled(-1.0, k, pm, nullptr);
-    for (int a = 0; a <= k; ++a) {
-      t.Ep[a] = pp[a];
-      t.Em[a] = pm[a];
+// The tables every kernel uses come from the generated compile-time constants of
+// wb_ctab.h (exact values rounded once), so the stage kernels (which fold them in as
+// immediates) and the auxiliary kernels (which read them from constant memory) agree to
+// the last bit.
+template <int K>
+static void fill_tab(Tab1D<double> &t) {
+  for (int a = 0; a < NQMAX; ++a) {
+    t.xq[a] = t.wq[a] = t.Ep[a] = t.Em[a] = 0.0;
+    for (int q = 0; q < NQMAX; ++q) t.B[a][q] = t.D[a][q] = t.BW[a][q] = t.DW[a][q] = 0.0;
+  }
+  for (int q = 0; q <= K; ++q) {
+    t.xq[q] = CTab<K>::xq(q);
+    t.wq[q] = CTab<K>::wq(q);
+    for (int a = 0; a <= K; ++a) {
+      t.B[a][q] = CTab<K>::B(a, q);
+      t.D[a][q] = CTab<K>::D(a, q);
+      t.BW[a][q] = CTab<K>::BW(a, q);
+      t.DW[a][q] = CTab<K>::DW(a, q);
     }
   }
+  for (int a = 0; a <= K; ++a) {
+    t.Ep[a] = CTab<K>::Ep(a);
+    t.Em[a] = CTab<K>::Em(a);
+  }
+}
+
+void make_tab1d(Tab1D<double> tabs[KMAX + 1]) {
+  static_assert(KMAX == 2, "tables generated for degrees 0..2");
+  fill_tab<0>(tabs[0]);
+  fill_tab<1>(tabs[1]);
+  fill_tab<2>(tabs[2]);
 }
 
 template <typename R>

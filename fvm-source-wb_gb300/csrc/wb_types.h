@@ -79,13 +79,15 @@ struct StageArgs {
   Combo<R> o[2];              // o[1].out may be null
   int nx, ny;
   long long plane;            // elements between (var, mode) planes
-  int bc_x, bc_y, llf_speed, limiter, lim_y;
+  int bc_x, bc_y, llf_speed, limiter, lim_y;  // limiter: 0 off, 1 minmod, 2 positivity
   int eq_kind;
   R dx, dy, hidx, hidy;       // hidx = 0.5/dx, hidy = 0.5/dy
   R gamma, gm1, igm1, hgam;   // hgam = gamma/(gamma-1)
   R gx, gy;
+  R gx4, gy4;                 // 0.25 gx, 0.25 gy (source weight of the assembly)
   R rho0, p0, kpoly, npoly;   // npoly = 1/(gamma-1)
   R lim_norm, lim_Mdx2, lim_Mdy2, lim_tol;
+  R pos_eps;                  // positivity limiter floor (limiter 2)
   // separable equilibrium factors: x at volume points [nx*nq], x at faces [nx+1], y likewise
   const R *fxv, *fxf, *fyv, *fyf;
   // time step
@@ -100,12 +102,16 @@ struct StageArgs {
   DevState *dev;
 };
 
-// Layout of one staged tile in shared memory (offsets in elements):
-//   su  [NV*NB][RY][RX]  modes of the tile and a one-cell halo
-//   sm  [NV][LY][LX]     means of the tile and a two-cell halo (limiter only)
-//   eq  fxv[NQ*TX], fxf[TX+1], fyv[NQ*TY], fyf[TY+1]  equilibrium factors
+// Layout of one staged tile in shared memory (offsets in elements).  Rows are stored with
+// pitch PX = TX + 8 starting at global column i0 - 4, so an x-interior row is one aligned
+// run of 16-byte chunks:
+//   su  [NV*NB][RY][PX]  modes of the tile and a one-cell halo (ring column rx at rx + 3)
+//   sm  [NV][LY][PX]     means of the tile and a two-cell halo (ring column lx at lx + 2;
+//                        limiter only)
+//   eq  fxv[NQ*(TX+2)], fxf[TX+1], fyv[NQ*(TY+2)], fyf[TY+1]  equilibrium factors (the
+//       volume-point factors cover the one-cell halo, for the positivity limiter)
 struct TileLayout {
-  int TX, TY, RX, RY, RXY, LX, LY, NB, NQ, lim;
+  int TX, TY, RX, RY, PX, RXY, LX, LY, NB, NQ, lim;
   int su, sm, eq, buf;
 };
 __host__ __device__ inline TileLayout tile_layout(int K, int basis, int TX, int TY, int lim) {
@@ -114,7 +120,8 @@ __host__ __device__ inline TileLayout tile_layout(int K, int basis, int TX, int 
   L.TY = TY;
   L.RX = TX + 2;
   L.RY = TY + 2;
-  L.RXY = L.RX * L.RY;
+  L.PX = TX + 8;
+  L.RXY = L.PX * L.RY;
   L.LX = TX + 4;
   L.LY = TY + 4;
   L.NB = num_modes(K, basis);
@@ -122,8 +129,8 @@ __host__ __device__ inline TileLayout tile_layout(int K, int basis, int TX, int 
   L.lim = lim;
   L.su = 0;
   L.sm = NV * L.NB * L.RXY;
-  L.eq = L.sm + (lim ? NV * L.LY * L.LX : 0);
-  const int neq = L.NQ * TX + TX + 1 + L.NQ * TY + TY + 1;
+  L.eq = L.sm + (lim ? NV * L.LY * L.PX : 0);
+  const int neq = L.NQ * (TX + 2) + TX + 1 + L.NQ * (TY + 2) + TY + 1;
   L.buf = (L.eq + neq + 3) & ~3;  // 16-byte aligned double buffers
   return L;
 }

@@ -48,6 +48,9 @@ extern "C" {
 #define WB_LLF_REF2D 1      /* lambda = max(|v_n+c|) as compute_llflux of 2d/benchmark_2d_dg.f90 */
 #define WB_PREC_FP64 0      /* "plain": FP64 state, literal F(u_eq+d) - F(u_eq) split */
 #define WB_PREC_FP32 1      /* FP64 equilibrium tables + FP32 perturbation, exact-difference fluxes */
+#define WB_LIMITER_NONE 0
+#define WB_LIMITER_MINMOD 1     /* limiter_type '1OR' (compute_limiter) on the perturbation */
+#define WB_LIMITER_POSITIVITY 2 /* limiter_type 'ONP' (compute_positivity) in delta form */
 #define WB_RK2 0            /* SSP-RK2 ('EQL' branch of evolve) */
 #define WB_RK54 1           /* SSP-RK(5,4) ('RK4' branch of evolve) */
 #define WB_LAYOUT_SOA 0
@@ -60,7 +63,9 @@ typedef struct {
   int32_t bc_x, bc_y;    /* WB_BC_* */
   int32_t eq_kind;       /* WB_EQ_* */
   int32_t llf_speed;     /* WB_LLF_* */
-  int32_t limiter;       /* 0 off, 1 minmod moment limiter on the perturbation */
+  int32_t limiter;       /* WB_LIMITER_*: 0 off, 1 minmod moment limiter on the perturbation
+                            (compute_limiter, 2d/limiters.f90:203-309), 2 Zhang-Shu
+                            positivity limiter (compute_positivity, :478-654) in delta form */
   int32_t precision;     /* WB_PREC_* */
   int32_t integrator;    /* WB_RK2 or WB_RK54 */
   int32_t tile_x, tile_y;/* CTA tile in cells; 0 = tuned default */
@@ -74,6 +79,7 @@ typedef struct {
   double lim_M;          /* TVB constant M (slopes with |norm s| < M h^2 untouched) */
   double lim_tol;        /* re-limit a cell only if a slope changes by more than this */
   double cfl;            /* CFL number */
+  double pos_eps;        /* positivity floor of density and pressure (reference eps 1e-10) */
 } wb_config;
 
 /* seeded perturbation generator (initial condition), evaluated on the device in FP64 */
@@ -109,6 +115,11 @@ int wb_download_state(wb_ctx *ctx, double *delta, int32_t layout);
 /* same with FP32 host arrays (SoA only) */
 int wb_upload_state_f32(wb_ctx *ctx, const float *delta);
 int wb_download_state_f32(wb_ctx *ctx, float *delta);
+/* The resident state exactly as stored (SoA; double for FP64 contexts, float for FP32),
+ * before the limit-on-load: what a checkpoint needs so that a restart through
+ * wb_upload_state / wb_upload_state_f32 continues bit for bit.  (No reference routine:
+ * the reference keeps its state in memory.) */
+int wb_download_state_raw(wb_ctx *ctx, void *delta);
 /* Projects a seeded perturbation onto the modes on the device (the IC + projection of
  * get_initial_conditions/get_modes_from_nodes, 2d/benchmark_2d_dg.f90:122-153,497-542);
  * resets t and the step counter. */
@@ -123,8 +134,9 @@ int wb_device_state(wb_ctx *ctx, void **dptr, size_t *plane_stride);
  * well-balanced split of compute_update_exact_delta, dg_with_source.f90:1749-2031.
  * The input is not limited (compute_update does not limit). */
 int wb_compute_update(wb_ctx *ctx, const double *delta_u, double *dudt, int32_t layout);
-/* Limits the resident state in place: apply_limiter(u), 2d/benchmark_2d_dg.f90:1516-1555
- * with compute_limiter, 2d/limiters.f90:203-309, applied to the perturbation. */
+/* Limits the resident state in place: apply_limiter(u), 2d/benchmark_2d_dg.f90:1516-1555,
+ * with compute_limiter (2d/limiters.f90:203-309) or compute_positivity (:478-654) as
+ * cfg.limiter selects, applied to the perturbation. */
 int wb_apply_limiter(wb_ctx *ctx);
 /* Directional maximum wave speeds max(|u|+c), max(|v|+c) over cell means of the full
  * state: compute_max_speed(u, cs_max, v_xmax, v_ymax, speed_max), :826-870. */
@@ -144,6 +156,12 @@ int wb_get_time(wb_ctx *ctx, double *t, int64_t *steps);
  * in evolve's locals and has no restart). */
 int wb_set_time(wb_ctx *ctx, double t, int64_t steps);
 
+/* Autotuner: times every compiled tile shape (CTA tile of cells) for this context's
+ * precision, degree, basis and grid over `steps` steps of the current state (restored
+ * afterwards), keeps the fastest and records it in the tile cache (the file named by the
+ * environment variable WB_TILE_CACHE, else tile_cache.txt beside the library), which
+ * wb_create consults when cfg->tile_x == 0.  No counterpart in the reference. */
+int wb_autotune(wb_ctx *ctx, int32_t steps, int32_t *tile_x, int32_t *tile_y);
 /* The context's CUDA stream (a cudaStream_t), for callers that order their own work
  * against it or time it with CUDA events.  No counterpart in the reference (serial). */
 int wb_get_stream(wb_ctx *ctx, void **stream);

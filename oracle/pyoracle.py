@@ -30,7 +30,7 @@ class OrcCfg(ctypes.Structure):
         ("rho0", ctypes.c_double), ("p0", ctypes.c_double), ("kpoly", ctypes.c_double),
         ("lx", ctypes.c_double), ("ly", ctypes.c_double),
         ("lim_norm", ctypes.c_double), ("lim_M", ctypes.c_double), ("lim_tol", ctypes.c_double),
-        ("cfl", ctypes.c_double),
+        ("cfl", ctypes.c_double), ("pos_eps", ctypes.c_double),
     ]
 
 
@@ -78,9 +78,13 @@ def lib():
         L.orc_nb.argtypes = [i, i]
         L.orc_modes.restype = i
         L.orc_modes.argtypes = [i, i, p, p]
-        for name in ("orc_rhs", "orc_limit"):
+        for name in ("orc_rhs", "orc_limit", "orc_positivity"):
             getattr(L, name).argtypes = [p, p, p]
         L.orc_project_ic.argtypes = [p, p, p]
+        L.orc_ref_positivity.argtypes = [p, p, p, i, p, p]
+        L.orc_solve_for_t.restype = d
+        L.orc_solve_for_t.argtypes = [p, p, p]
+        L.orc_eq_modes.argtypes = [p, i, i, p, p]
         L.orc_nodes_from_modes.argtypes = [p, i, p, p]
         L.orc_modes_from_nodes.argtypes = [p, i, p, p]
         L.orc_max_speed.argtypes = [p, p, p, p]
@@ -115,12 +119,13 @@ def _ptr(a):
 def make_cfg(nx=16, ny=16, order=1, basis=BASIS_P, bc_x=BC_COPY, bc_y=BC_COPY,
              eq_kind=EQ_ISOTHERMAL, llf_speed=LLF_MAXABS, limiter=0, gamma=1.4, gx=1.0, gy=1.0,
              rho0=1.0, p0=1.0, kpoly=1.0, lx=1.0, ly=1.0, lim_norm=3.0, lim_M=0.0,
-             lim_tol=1e-6, cfl=0.3):
+             lim_tol=1e-6, cfl=0.3, pos_eps=1e-10):
     c = OrcCfg()
     c.nx, c.ny, c.order, c.basis = nx, ny, order, basis
     c.bc_x, c.bc_y, c.eq_kind, c.llf_speed, c.limiter = bc_x, bc_y, eq_kind, llf_speed, limiter
     c.gamma, c.gx, c.gy, c.rho0, c.p0, c.kpoly = gamma, gx, gy, rho0, p0, kpoly
     c.lx, c.ly, c.lim_norm, c.lim_M, c.lim_tol, c.cfl = lx, ly, lim_norm, lim_M, lim_tol, cfl
+    c.pos_eps = pos_eps
     return c
 
 
@@ -146,6 +151,11 @@ def state_shape(cfg):
 
 def zeros(cfg):
     return np.zeros(state_shape(cfg), dtype=np.float64)
+
+
+def legendre(x, n):
+    """phi_n(x) = sqrt(2n+1) P_n(x) (2d/legendre.f90:1-25)"""
+    return lib().orc_legendre(float(x), int(n))
 
 
 def gl(n):
@@ -175,6 +185,46 @@ def rhs(cfg, delta):
     delta = np.ascontiguousarray(delta, dtype=np.float64)
     out = np.empty_like(delta)
     lib().orc_rhs(ctypes.byref(cfg), _ptr(delta), _ptr(out))
+    return out
+
+
+def positivity(cfg, delta):
+    """Zhang-Shu positivity limiter in delta form (whatever cfg.limiter says)."""
+    delta = np.ascontiguousarray(delta, dtype=np.float64)
+    out = np.empty_like(delta)
+    lib().orc_positivity(ctypes.byref(cfg), _ptr(delta), _ptr(out))
+    return out
+
+
+def ref_positivity(cfg, u_full, ref_gll_nodes=False):
+    """Literal compute_positivity on full-state modes; returns (u, theta, t) per cell."""
+    u_full = np.ascontiguousarray(u_full, dtype=np.float64)
+    out = np.empty_like(u_full)
+    nc = cfg.nx * cfg.ny
+    th = np.ones(nc)
+    tt = np.ones(nc)
+    lib().orc_ref_positivity(ctypes.byref(cfg), _ptr(u_full), _ptr(out), int(ref_gll_nodes),
+                             _ptr(th), _ptr(tt))
+    return out, th.reshape(cfg.ny, cfg.nx), tt.reshape(cfg.ny, cfg.nx)
+
+
+def solve_for_t(cfg, u, u_avg):
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    ua = np.ascontiguousarray(u_avg, dtype=np.float64)
+    return lib().orc_solve_for_t(ctypes.byref(cfg), _ptr(u), _ptr(ua))
+
+
+def eq_modes_full(cfg):
+    """Projected equilibrium as a full state (4, nb, ny, nx): rho and E modes, zero momentum."""
+    n = nb(cfg)
+    out = np.zeros((4, n, cfg.ny, cfg.nx))
+    er = np.zeros(n)
+    ee = np.zeros(n)
+    for j in range(cfg.ny):
+        for i in range(cfg.nx):
+            lib().orc_eq_modes(ctypes.byref(cfg), i, j, _ptr(er), _ptr(ee))
+            out[0, :, j, i] = er
+            out[3, :, j, i] = ee
     return out
 
 

@@ -546,8 +546,12 @@ void orc_limit(const orc_cfg *c, const double *in, double *out) {
   make_tabs(c, &t);
   const int nx = c->nx, ny = c->ny, nb = t.nb;
   const size_t nc = (size_t)nx * ny;
+  if (c->limiter == 2) {
+    orc_positivity(c, in, out);
+    return;
+  }
   memcpy(out, in, sizeof(double) * nc * NV * nb);
-  if (!c->limiter || c->order < 1) return;
+  if (c->limiter != 1 || c->order < 1) return;
   const int m10 = t.idx[1][0], m01 = t.idx[0][1];
   const double nrm = c->lim_norm;
 #pragma omp parallel for num_threads(g_threads) schedule(static)
@@ -573,6 +577,167 @@ void orc_limit(const orc_cfg *c, const double *in, double *out) {
         }
       }
     }
+}
+
+/* ------------------------------------------------ positivity limiter */
+
+/* GLL nodes used by compute_set: gll = (2*(mx-1)+3)/2 points (2d/parameters_dg_2d.f90:7)
+ * from gll_quadrature (2d/legendre.f90:111-170).  The reference lists -1 and 0 for its
+ * two-point rule (:122-126); ref != 0 keeps that, otherwise the Lobatto nodes -1, +1. */
+static int gll_nodes(int k, int ref, double *xg) {
+  const int n = (2 * k + 3) / 2;
+  switch (n) {
+  case 2: xg[0] = -1.0; xg[1] = ref ? 0.0 : 1.0; break;
+  case 3: xg[0] = -1.0; xg[1] = 0.0; xg[2] = 1.0; break;
+  case 4:
+    xg[0] = -1.0; xg[1] = -1.0 / 5.0 * sqrt(5.0); xg[2] = 1.0 / 5.0 * sqrt(5.0); xg[3] = 1.0;
+    break;
+  default: return 0;
+  }
+  return n;
+}
+
+/* compute_set (2d/limiters.f90:438-475): the cell polynomial at (GLL x GL) and (GL x GLL);
+ * val[v][p], p = q*ng + g for the first family and nq*ng + q*ng + g for the second. */
+static int positivity_set(const tabs_t *t, int ng, const double *xg, double W[NV][NBMAX],
+                          double val[NV][2 * NQMAX * 4]) {
+  for (int q = 0; q < t->nq; ++q)
+    for (int g = 0; g < ng; ++g) {
+      const int p1 = q * ng + g, p2 = t->nq * ng + q * ng + g;
+      for (int v = 0; v < NV; ++v) {
+        double s1 = 0.0, s2 = 0.0;
+        for (int m = 0; m < t->nb; ++m) {
+          s1 = s1 + W[v][m] * orc_legendre(xg[g], t->ma[m]) * orc_legendre(t->xq[q], t->mb[m]);
+          s2 = s2 + W[v][m] * orc_legendre(t->xq[q], t->ma[m]) * orc_legendre(xg[g], t->mb[m]);
+        }
+        val[v][p1] = s1;
+        val[v][p2] = s2;
+      }
+    }
+  return 2 * t->nq * ng;
+}
+
+/* solve_for_t, 2d/limiters.f90:312-362: the root in [0,1] of p(u_avg + t (u - u_avg)) = eps,
+ * written as a t^2 + b t + c = 0 with (2 rho E - |m|^2 - 2 eps rho/(gamma-1)) */
+double orc_solve_for_t(const orc_cfg *c, const double *u, const double *ua) {
+  const double eps = c->pos_eps, g = c->gamma;
+  const double pa = ua[0], mxa = ua[1], mya = ua[2], ea = ua[3];
+  const double pj = u[0], mxj = u[1], myj = u[2], ej = u[3];
+  double a = 2.0 * (pj - pa) * (ej - ea) - (mxj - mxa) * (mxj - mxa) - (myj - mya) * (myj - mya);
+  double b = 2.0 * (pj - pa) * (ea - eps / (g - 1)) + 2.0 * pa * (ej - ea) -
+             2.0 * (mxa * (mxj - mxa) + mya * (myj - mya));
+  double cc = 2.0 * pa * ea - (mxa * mxa + mya * mya) - 2.0 * eps * pa / (g - 1.0);
+  b = b / a;
+  cc = cc / a;
+  const double D = sqrt(fabs(b * b - 4 * cc));
+  const double t1 = 0.5 * (-b - D), t2 = 0.5 * (-b + D);
+  double t;
+  if ((t1 > -eps) && (t1 < 1.0 + eps)) t = t1;
+  else if ((t2 > -eps) && (t2 < 1.0 + eps)) t = t2;
+  else t = 0.0;
+  t = fmin(1.0, t);
+  t = fmax(0.0, t);
+  return t;
+}
+
+/* compute_positivity on one cell (2d/limiters.f90:478-654): density first (theta scales the
+ * non-mean density modes), then pressure on the density-limited set (t_min scales the
+ * non-mean modes of every variable).  u_avg is the cell's mode (0,0). */
+static void positivity_cell(const orc_cfg *c, const tabs_t *t, int ng, const double *xg,
+                            double W[NV][NBMAX], double *theta_out, double *t_out) {
+  const double eps = c->pos_eps;
+  double val[NV][2 * NQMAX * 4], ua[NV];
+  for (int v = 0; v < NV; ++v) ua[v] = W[v][0];
+  int np = positivity_set(t, ng, xg, W, val);
+  double pmin = val[0][0];
+  for (int p = 1; p < np; ++p) pmin = fmin(pmin, val[0][p]);
+  const double theta = fmin(fabs((ua[0] - eps) / (ua[0] - pmin)), 1.0);
+  for (int m = 1; m < t->nb; ++m) W[0][m] = theta * W[0][m];
+  np = positivity_set(t, ng, xg, W, val);
+  double tmin = 1.0;
+  for (int p = 0; p < np; ++p) {
+    double u[NV], w[NV], tt;
+    for (int v = 0; v < NV; ++v) u[v] = val[v][p];
+    prim(c->gamma, u, w);
+    if (w[3] > eps) tt = 1.0;
+    else tt = orc_solve_for_t(c, u, ua);
+    if (tmin >= tt) tmin = tt;
+  }
+  for (int v = 0; v < NV; ++v)
+    for (int m = 1; m < t->nb; ++m) W[v][m] = tmin * W[v][m];
+  if (theta_out) *theta_out = theta;
+  if (t_out) *t_out = tmin;
+}
+
+void orc_ref_positivity(const orc_cfg *c, const double *in, double *out, int ref_gll,
+                        double *theta_out, double *t_out) {
+  tabs_t t;
+  make_tabs(c, &t);
+  const size_t nc = (size_t)c->nx * c->ny;
+  memcpy(out, in, sizeof(double) * nc * NV * t.nb);
+  double xg[4];
+  const int ng = gll_nodes(c->order, ref_gll, xg);
+  if (c->order < 1 || ng == 0) return;  /* mx == 1: no limiting (:519-523) */
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+  for (size_t cell = 0; cell < nc; ++cell) {
+    double W[NV][NBMAX], th, tm;
+    for (int v = 0; v < NV; ++v)
+      for (int m = 0; m < t.nb; ++m) W[v][m] = in[((size_t)v * t.nb + m) * nc + cell];
+    positivity_cell(c, &t, ng, xg, W, &th, &tm);
+    for (int v = 0; v < NV; ++v)
+      for (int m = 0; m < t.nb; ++m) out[((size_t)v * t.nb + m) * nc + cell] = W[v][m];
+    if (theta_out) theta_out[cell] = th;
+    if (t_out) t_out[cell] = tm;
+  }
+}
+
+static void eq_modes_t(const orc_cfg *c, const tabs_t *t, int i, int j, double *er, double *ee) {
+  const double igm1 = 1.0 / (c->gamma - 1.0);
+  for (int m = 0; m < t->nb; ++m) {
+    double r = 0.0, e = 0.0;
+    for (int qa = 0; qa < t->nq; ++qa)
+      for (int qb = 0; qb < t->nq; ++qb) {
+        double re, pe;
+        orc_eq_point(c, eq_fx(c, xvol(t, i, qa)), eq_fy(c, yvol(t, j, qb)), 0, 0, &re, &pe);
+        const double w = 0.25 * t->wq[qa] * t->wq[qb] * t->B[t->ma[m]][qa] * t->B[t->mb[m]][qb];
+        r = r + re * w;
+        e = e + pe * igm1 * w;
+      }
+    er[m] = r;
+    ee[m] = e;
+  }
+}
+void orc_eq_modes(const orc_cfg *c, int i, int j, double *e_rho, double *e_E) {
+  tabs_t t;
+  make_tabs(c, &t);
+  eq_modes_t(c, &t, i, j, e_rho, e_E);
+}
+
+void orc_positivity(const orc_cfg *c, const double *in, double *out) {
+  tabs_t t;
+  make_tabs(c, &t);
+  const int nx = c->nx;
+  const size_t nc = (size_t)nx * c->ny;
+  memcpy(out, in, sizeof(double) * nc * NV * t.nb);
+  double xg[4];
+  const int ng = gll_nodes(c->order, 0, xg);
+  if (c->order < 1 || ng == 0) return;
+#pragma omp parallel for num_threads(g_threads) schedule(static)
+  for (size_t cell = 0; cell < nc; ++cell) {
+    double W[NV][NBMAX], er[NBMAX], ee[NBMAX], th, tm;
+    eq_modes_t(c, &t, (int)(cell % nx), (int)(cell / nx), er, ee);
+    for (int v = 0; v < NV; ++v)
+      for (int m = 0; m < t.nb; ++m) {
+        const double d = in[((size_t)v * t.nb + m) * nc + cell];
+        W[v][m] = v == 0 ? er[m] + d : v == 3 ? ee[m] + d : d;
+      }
+    positivity_cell(c, &t, ng, xg, W, &th, &tm);
+    if (th < 1.0 || tm < 1.0)
+      for (int v = 0; v < NV; ++v)
+        for (int m = 1; m < t.nb; ++m)
+          out[((size_t)v * t.nb + m) * nc + cell] =
+              v == 0 ? W[v][m] - er[m] : v == 3 ? W[v][m] - ee[m] : W[v][m];
+  }
 }
 
 /* cell-mean equilibrium (mode (0,0) of its projection, 2d/benchmark_2d_dg.f90:530-536) */

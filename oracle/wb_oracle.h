@@ -35,7 +35,8 @@ typedef struct {
   int bc_x, bc_y;    /* ORC_BC_* */
   int eq_kind;       /* ORC_EQ_* */
   int llf_speed;     /* ORC_LLF_* wave-speed estimate */
-  int limiter;       /* 0 off, 1 minmod moment limiter on the perturbation */
+  int limiter;       /* 0 off, 1 minmod moment limiter on the perturbation,
+                        2 Zhang-Shu positivity limiter (in delta form) */
   int pad0;
   double gamma;
   double gx, gy;     /* constant gravity: Phi = gx*x + gy*y */
@@ -46,6 +47,7 @@ typedef struct {
   double lim_M;      /* TVB constant: slopes with |norm*s| < M*dx^2 are left alone */
   double lim_tol;    /* a cell is re-limited only if a slope changes by more than this */
   double cfl;
+  double pos_eps;    /* positivity floor of density and pressure (reference eps = 1e-10) */
 } orc_cfg;
 
 /* perturbation (initial condition) description; shared meaning with the product's */
@@ -84,6 +86,21 @@ void orc_project_ic(const orc_cfg *c, const orc_ic *ic, double *delta);
 /* ---- the composed 2D well-balanced DG operator, FP64 literal delta-split ---- */
 void orc_rhs(const orc_cfg *c, const double *delta, double *dudt);
 void orc_limit(const orc_cfg *c, const double *in, double *out);
+/* Zhang-Shu positivity limiter in delta form: compute_positivity (2d/limiters.f90:478-654)
+ * applied to the full-state polynomial e + delta (e = the cell's projected equilibrium);
+ * writes delta back.  Cells left untouched by the limiter are copied bit for bit. */
+void orc_positivity(const orc_cfg *c, const double *in, double *out);
+/* The literal compute_positivity on full-state modes (SoA, this file's mode order).
+ * ref_gll_nodes != 0 takes the reference's two-point GLL node list {-1, 0}
+ * (2d/legendre.f90:122-126) for degree 1; 0 takes the Lobatto nodes {-1, +1}.
+ * theta_out / t_out (may be NULL) receive each cell's density and pressure factors. */
+void orc_ref_positivity(const orc_cfg *c, const double *u_in, double *u_out,
+                        int ref_gll_nodes, double *theta_out, double *t_out);
+/* solve_for_t, 2d/limiters.f90:312-362 (u and u_avg: rho, mx, my, E) */
+double orc_solve_for_t(const orc_cfg *c, const double *u, const double *u_avg);
+/* Projected equilibrium (rho and E modes) of cell (i, j): get_modes_from_nodes
+ * (2d/benchmark_2d_dg.f90:497-542) of the equilibrium at the GL points. */
+void orc_eq_modes(const orc_cfg *c, int i, int j, double *e_rho, double *e_E);
 void orc_max_speed(const orc_cfg *c, const double *delta, double *smax_x, double *smax_y);
 double orc_cfl_dt(const orc_cfg *c, double smax_x, double smax_y);
 /* nsteps SSP-RK2 steps; dt_fixed > 0 uses that dt, else CFL dt each step.

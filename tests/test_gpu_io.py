@@ -2,28 +2,34 @@
 import numpy as np
 import pytest
 
-from helpers import base_cfg, orc_cfg, random_delta, solver
+from helpers import base_cfg, orc_cfg, random_delta, solver, violating_delta
 
 pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("precision", [0, 1])
-@pytest.mark.parametrize("limiter", [0, 1])
+@pytest.mark.parametrize("limiter", [0, 1, 2])
 def test_restart_is_bitwise(wb, tmp_path, precision, limiter):
     c = base_cfg(nx=20, ny=16, order=2, basis=1, limiter=limiter, bc_x=0)
-    # rough data only with the limiter on (unlimited P2 steps of rough data go non-physical)
-    d = random_delta(c, amp=3e-2 if limiter else 5e-3, seed=4, smooth=not limiter)
+    # rough data only with the limiter on (unlimited P2 steps of rough data go non-physical);
+    # the positivity limiter gets a state that violates positivity, and fixed steps
+    if limiter == 2:
+        d = violating_delta(c, seed=4, ncells=6, depth=1.0)
+        dt = 2e-4
+    else:
+        d = random_delta(c, amp=3e-2 if limiter else 5e-3, seed=4, smooth=not limiter)
+        dt = -1.0
     with solver(wb, c, precision) as a:
         a.upload(d)
-        a.step(10)
+        a.step(10, dt)
         ref = a.download()
         tref, nref = a.time()
     with solver(wb, c, precision) as b:
         b.upload(d)
-        b.step(5)
+        b.step(5, dt)
         b.save_checkpoint(str(tmp_path / "ck.bin"))
     r = wb.Solver.from_checkpoint(str(tmp_path / "ck.bin"))
-    r.step(5)
+    r.step(5, dt)
     got = r.download()
     t, n = r.time()
     r.close()
@@ -57,3 +63,23 @@ def test_output_file_format(wb, orc, tmp_path):
                  0.4 * (u[3] - 0.5 * (u[1] ** 2 + u[2] ** 2) / u[0]) - pe]
             np.testing.assert_allclose(vals, [xq, yq] + w, rtol=1e-5, atol=1e-16)
             k += 1
+
+
+def test_autotune_preserves_state(wb, tmp_path, monkeypatch):
+    monkeypatch.setenv("WB_TILE_CACHE", str(tmp_path / "tiles.txt"))
+    c = base_cfg(nx=64, ny=48, order=2, basis=1, limiter=1)
+    d = random_delta(c, amp=1e-2, seed=12)
+    with solver(wb, c, 1) as s:
+        s.upload(d)
+        s.step(2)
+        before = s.download()
+        t0 = s.time()
+        tx, ty = s.autotune(2)
+        assert (tx, ty) in [(32, 8), (16, 16)]
+        np.testing.assert_array_equal(s.download(), before)
+        assert s.time() == t0
+    lines = open(tmp_path / "tiles.txt").read().split()
+    assert [int(v) for v in lines[-2:]] == [tx, ty]
+    with solver(wb, c, 1) as s2:   # a new context picks the cached shape up
+        s2.upload(d)
+        assert s2.autotune(1) in [(32, 8), (16, 16)]
