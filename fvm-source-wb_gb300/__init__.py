@@ -26,6 +26,7 @@ LLF_MAXABS, LLF_REF2D = 0, 1
 PREC_FP64, PREC_FP32 = 0, 1
 RK2, RK54 = 0, 1
 LIMITER_NONE, LIMITER_MINMOD, LIMITER_POSITIVITY = 0, 1, 2
+RIEMANN_LLF, RIEMANN_HLLC = 0, 1
 LAYOUT_SOA, LAYOUT_FORTRAN = 0, 1
 
 
@@ -38,7 +39,7 @@ class WbError(RuntimeError):
 class WbConfig(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int32) for n in (
         "nx", "ny", "order", "basis", "bc_x", "bc_y", "eq_kind", "llf_speed", "limiter",
-        "precision", "integrator", "tile_x", "tile_y", "device")] + [
+        "precision", "integrator", "tile_x", "tile_y", "device", "riemann", "reserved")] + [
         (n, ctypes.c_double) for n in (
             "gamma", "gx", "gy", "rho0", "p0", "kpoly", "lx", "ly", "lim_norm", "lim_M",
             "lim_tol", "cfl", "pos_eps")]

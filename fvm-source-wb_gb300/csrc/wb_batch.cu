@@ -131,6 +131,8 @@ int wb_batch_create(const wb_config *cfgs, int32_t n, wb_batch **out) {
                   "batch instances must be FP32-perturbation, SSP-RK2, total-degree basis, one device");
     if (c.tile_x > 0 && (c.tile_x != 32 || c.tile_y != 8))
       return berr(b, WB_ERR_CONFIG, "the batch runs 32x8 tiles");
+    if (c.riemann != WB_RIEMANN_LLF)
+      return berr(b, WB_ERR_CONFIG, "the batch runs the LLF flux");
   }
   BCK(cudaSetDevice(b->device));
   BCK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));

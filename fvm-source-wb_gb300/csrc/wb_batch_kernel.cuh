@@ -68,9 +68,9 @@ __global__ void __launch_bounds__(256, 2)
       S->smax[A.parity ^ 1][1] = 0ull;
     }
     const bool lim = A.limiter == 1 && A.lim_y && K >= 1;
-    if (K == 0) tile_compute<R, 0, 1, BATCH_TX, BATCH_TY, POS>(A, lim, w.y, w.z, buf, flux, red, tid, dt);
-    else if (K == 1) tile_compute<R, 1, 1, BATCH_TX, BATCH_TY, POS>(A, lim, w.y, w.z, buf, flux, red, tid, dt);
-    else tile_compute<R, 2, 1, BATCH_TX, BATCH_TY, POS>(A, lim, w.y, w.z, buf, flux, red, tid, dt);
+    if (K == 0) tile_compute<R, 0, 1, BATCH_TX, BATCH_TY, POS ? WB_VAR_POSITIVITY : 0>(A, lim, w.y, w.z, buf, flux, red, tid, dt);
+    else if (K == 1) tile_compute<R, 1, 1, BATCH_TX, BATCH_TY, POS ? WB_VAR_POSITIVITY : 0>(A, lim, w.y, w.z, buf, flux, red, tid, dt);
+    else tile_compute<R, 2, 1, BATCH_TX, BATCH_TY, POS ? WB_VAR_POSITIVITY : 0>(A, lim, w.y, w.z, buf, flux, red, tid, dt);
     const int in = it + 2 * (int)gridDim.x;
     if (in < nitems) item_load(args, items[in], sA[k & 1], buf, tid, nthr);
     cp_async_commit();

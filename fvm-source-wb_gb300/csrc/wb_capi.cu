@@ -77,6 +77,8 @@ int validate(const wb_config *c, std::string &why) {
     double phimax = std::fmax(0.0, c->gx * c->lx) + std::fmax(0.0, c->gy * c->ly);
     if (!(1.0 - k * phimax > 0.0)) return why = "polytrope density vanishes inside the domain", WB_ERR_CONFIG;
   }
+  if (c->riemann != WB_RIEMANN_LLF && c->riemann != WB_RIEMANN_HLLC)
+    return why = "bad riemann (0 LLF, 1 HLLC)", WB_ERR_CONFIG;
   if (c->limiter < 0 || c->limiter > 2) return why = "bad limiter (0 off, 1 minmod, 2 positivity)", WB_ERR_CONFIG;
   if (c->limiter == 1 && !(c->lim_norm > 0.0)) return why = "lim_norm must be > 0", WB_ERR_CONFIG;
   if (c->limiter == 2 && !(c->pos_eps > 0.0)) return why = "pos_eps must be > 0", WB_ERR_CONFIG;
@@ -103,6 +105,7 @@ StageArgs<R> base_args(const wb_ctx *c) {
   A.llf_speed = g.llf_speed;
   A.limiter = g.limiter;
   A.lim_y = 1;
+  A.riemann = g.riemann;
   A.eq_kind = g.eq_kind;
   double dx = g.lx / g.nx, dy = g.ly / g.ny;
   A.dx = (R)dx;
@@ -509,6 +512,7 @@ int wb_config_default(wb_config *c) {
   c->lim_tol = 1e-6;    // 2d/limiters.f90:262
   c->cfl = 0.2;         // 2d/parameters_dg_2d.f90:26
   c->pos_eps = 1e-10;   // eps, 2d/parameters_dg_2d.f90:28
+  c->riemann = WB_RIEMANN_LLF;  // flux_type = 'llf' (2d/parameters_dg_2d.f90:15)
   return WB_OK;
 }
 

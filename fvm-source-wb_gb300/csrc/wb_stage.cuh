@@ -175,12 +175,20 @@ __device__ __forceinline__ void vol_point(const StageArgs<R> &A, const R *d, R r
   }
 }
 
-// Face point in direction DIR: LLF flux difference (F_hat - F(u_eq)) from perturbation
-// traces dL (left/bottom) and dR (right/top) on the equilibrium face state.
-// compute_llflux, 2d/benchmark_2d_dg.f90:968-988.
-template <typename R, int DIR>
+// Face point in direction DIR: numerical flux minus the equilibrium flux, F_hat - F(u_eq),
+// from perturbation traces dL (left/bottom) and dR (right/top) on the equilibrium face
+// state.  LLF: compute_llflux, 2d/benchmark_2d_dg.f90:968-988.  HLLC (compile-time switch):
+// riemann_hllc, dg_with_source.f90:1318-1374, with Davis wave speeds, the contact speed
+// from the Lagrangian sound speeds, the transverse velocity carried by the contact, and
+// the star fluxes in the form F_K + S_K (U*_K - U_K),
+//   U*_K - U_K = (S* - v_K) / (S_K - S*) [rho_K, rho_K S_K, rho_K vt_K, E_K + p_K + rho_K S* (S_K - v_K)],
+// which is riemann_hllc's F(U*_K) in exact arithmetic.  Every star correction carries the
+// factor S* - v_K, which is exactly zero for a zero perturbation, so both forms keep the
+// equilibrium exactly.
+template <typename R, int DIR, bool HLLC>
 __device__ __forceinline__ void face_point(const StageArgs<R> &A, const R *dL, const R *dR, R re,
                                            R pe, R *F) {
+  constexpr int N = 1 + DIR, T = 2 - DIR;  // normal and transverse momentum
   if constexpr (std::is_same<R, double>::value) {
     double ue[NV] = {re, 0.0, 0.0, pe * A.igm1}, uL[NV], uR[NV], wL[NV], wR[NV], we[NV];
     double fL[NV], fR[NV], fe[NV];
@@ -197,15 +205,44 @@ __device__ __forceinline__ void face_point(const StageArgs<R> &A, const R *dL, c
     flux_lit<DIR>(ue, we, fe);
     double cL = sqrt(A.gamma * fmax(wL[3], 1e-10) / fmax(wL[0], 1e-10));
     double cR = sqrt(A.gamma * fmax(wR[3], 1e-10) / fmax(wR[0], 1e-10));
-    double vL = wL[1 + DIR], vR = wR[1 + DIR], lam;
-    if (A.llf_speed == 1)
-      lam = fmax(fabs(vR + cR), fabs(vL + cL));
-    else
-      lam = fmax(fabs(vL) + cL, fabs(vR) + cR);
+    double vL = wL[N], vR = wR[N];
+    if constexpr (HLLC) {
+      const double SL = fmin(vL, vR) - fmax(cL, cR), SR = fmax(vL, vR) + fmax(cL, cR);
+      const double DL = wL[0] * (vL - SL), DR = wR[0] * (SR - vR);
+      const double Ss = (DR * vR + DL * vL + (wL[3] - wR[3])) / (DL + DR);
+      if (SL > 0.0) {
 #pragma unroll
-    for (int v = 0; v < NV; ++v) F[v] = (0.5 * (fR[v] + fL[v]) + 0.5 * lam * (uL[v] - uR[v])) - fe[v];
+        for (int v = 0; v < NV; ++v) F[v] = fL[v] - fe[v];
+      } else if (!(Ss > 0.0) && !(SR > 0.0)) {
+#pragma unroll
+        for (int v = 0; v < NV; ++v) F[v] = fR[v] - fe[v];
+      } else {  // the star regions, sampled in riemann_hllc's order
+        const bool left = Ss > 0.0;
+        const double *u = left ? uL : uR, *w = left ? wL : wR, *f = left ? fL : fR;
+        const double SK = left ? SL : SR, vK = w[N];
+        const double q = SK * ((Ss - vK) / (SK - Ss));
+        double d[NV];
+        d[0] = w[0];
+        d[N] = w[0] * SK;
+        d[T] = w[0] * w[T];
+        d[3] = (u[3] + w[3]) + w[0] * Ss * (SK - vK);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) F[v] = (f[v] + q * d[v]) - fe[v];
+      }
+    } else {
+      double lam;
+      if (A.llf_speed == 1)
+        lam = fmax(fabs(vR + cR), fabs(vL + cL));
+      else
+        lam = fmax(fabs(vL) + cL, fabs(vR) + cR);
+#pragma unroll
+      for (int v = 0; v < NV; ++v)
+        F[v] = (0.5 * (fR[v] + fL[v]) + 0.5 * lam * (uL[v] - uR[v])) - fe[v];
+    }
   } else {
-    R fL[NV], fR[NV], lamL, lamR;
+    // exact-difference side quantities: r = rho, vn / vt = normal / transverse velocity,
+    // dp = pressure perturbation, H = E + p of the full state, f = flux difference
+    R fL[NV], fR[NV], lamL, lamR, rs[2], vns[2], vts[2], dps[2], Hs[2], cs[2];
     R hp = A.hgam * pe;
 #pragma unroll
     for (int s = 0; s < 2; ++s) {
@@ -222,12 +259,42 @@ __device__ __forceinline__ void face_point(const StageArgs<R> &A, const R *dL, c
       f[2] = DIR == 0 ? d[2] * vx : d[2] * vy + dp;
       f[3] = vn * H;
       R c = fsqrt_pos(A.gamma * rfmax(pe + dp, R(1e-10)) * inv);
+      rs[s] = r;
+      vns[s] = vn;
+      vts[s] = DIR == 0 ? vy : vx;
+      dps[s] = dp;
+      Hs[s] = H;
+      cs[s] = c;
       R lam = A.llf_speed == 1 ? vn + c : fabs(vn) + c;
       if (s == 0) lamL = lam; else lamR = lam;
     }
-    R lam = A.llf_speed == 1 ? rfmax(fabs(lamR), fabs(lamL)) : rfmax(lamL, lamR);
+    if constexpr (HLLC) {
+      const R SL = fmin(vns[0], vns[1]) - fmax(cs[0], cs[1]);
+      const R SR = fmax(vns[0], vns[1]) + fmax(cs[0], cs[1]);
+      const R DL = rs[0] * (vns[0] - SL), DR = rs[1] * (SR - vns[1]);
+      // p_L - p_R = dp_L - dp_R: the equilibrium pressure is the same on both sides
+      const R Ss = (DR * vns[1] + DL * vns[0] + (dps[0] - dps[1])) / (DL + DR);
+      if (SL > R(0)) {
 #pragma unroll
-    for (int v = 0; v < NV; ++v) F[v] = R(0.5) * (fR[v] + fL[v]) + R(0.5) * lam * (dL[v] - dR[v]);
+        for (int v = 0; v < NV; ++v) F[v] = fL[v];
+      } else if (!(Ss > R(0)) && !(SR > R(0))) {
+#pragma unroll
+        for (int v = 0; v < NV; ++v) F[v] = fR[v];
+      } else {  // the star regions, sampled in riemann_hllc's order
+        const int k = Ss > R(0) ? 0 : 1;
+        const R SK = k == 0 ? SL : SR, vK = vns[k], r = rs[k];
+        const R q = SK * ((Ss - vK) / (SK - Ss));
+        const R *f = k == 0 ? fL : fR;
+        F[0] = f[0] + q * r;
+        F[N] = f[N] + q * (r * SK);
+        F[T] = f[T] + q * (r * vts[k]);
+        F[3] = f[3] + q * (Hs[k] + r * Ss * (SK - vK));
+      }
+    } else {
+      R lam = A.llf_speed == 1 ? rfmax(fabs(lamR), fabs(lamL)) : rfmax(lamL, lamR);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) F[v] = R(0.5) * (fR[v] + fL[v]) + R(0.5) * lam * (dL[v] - dR[v]);
+    }
   }
 }
 
@@ -500,12 +567,14 @@ __device__ __forceinline__ void tile_load_async(const StageArgs<R> &A, const boo
 // Compute one staged tile: limiter, face fluxes, cell quadrature, RK combination and the
 // wave-speed reduction.  Thread tid owns cell (tid % TX, tid / TX).  Ends with a CTA
 // barrier, after which `buf` and the flux area may be reused.
-template <typename R, int K, int BASIS, int TX, int TY, bool POS>
+template <typename R, int K, int BASIS, int TX, int TY, int VAR>
 __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool lim_,
                                              const int i0, const int j0, R *buf, R *flux,
                                              double *red, const int tid, const double dt) {
   constexpr int NQ = K + 1;
   constexpr int NB = num_modes(K, BASIS);
+  constexpr bool POS = (VAR & WB_VAR_POSITIVITY) != 0;  // positivity limiter compiled in
+  constexpr bool HLLC = (VAR & WB_VAR_HLLC) != 0;       // HLLC face flux (else LLF)
   using T = TC<R, K>;
   const TileLayout L = tile_layout(K, BASIS, TX, TY, lim_);
   // RX / LX below are the stored row pitch (TX + 8); the staged ring starts at column 3
@@ -598,7 +667,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
         dR[v] = sr;
       }
       eq_point(A, fxf, sfyv[fj * NQ + q], re, pe);
-      face_point<R, 0>(A, dL, dR, re, pe, F);
+      face_point<R, 0, HLLC>(A, dL, dR, re, pe, F);
 #pragma unroll
       for (int v = 0; v < NV; ++v)
 #pragma unroll
@@ -648,7 +717,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
         dT[v] = st;
       }
       eq_point(A, sfxv[fi * NQ + q], fyf, re, pe);
-      face_point<R, 1>(A, dB, dT, re, pe, F);
+      face_point<R, 1, HLLC>(A, dB, dT, re, pe, F);
 #pragma unroll
       for (int v = 0; v < NV; ++v)
 #pragma unroll
@@ -854,9 +923,9 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
 // Persistent stage kernel: CTAs stride over the tiles of the grid; the next-but-one
 // tile is staged by cp.async while the current one is computed (double buffering).
 // The tile shape is a compile-time parameter so all shared-memory indexing folds.
-// POS compiles the positivity limiter in (limiter 2); without it the kernel carries no
-// positivity code at all.
-template <typename R, int K, int BASIS, int TX, int TY, bool POS>
+// VAR selects compile-time variants (WB_VAR_*): the positivity limiter (limiter 2) and the
+// HLLC face flux; the default kernel carries neither.
+template <typename R, int K, int BASIS, int TX, int TY, int VAR>
 __global__ void __launch_bounds__(TX *TY, std::is_same<R, float>::value ? 2 : 1)
     k_stage(const __grid_constant__ StageArgs<R> A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -887,7 +956,7 @@ __global__ void __launch_bounds__(TX *TY, std::is_same<R, float>::value ? 2 : 1)
     cp_async_wait<1>();
     __syncthreads();
     R *buf = bufs + (k & 1) * L.buf;
-    tile_compute<R, K, BASIS, TX, TY, POS>(A, lim, (t % ntx) * TX, (t / ntx) * TY, buf, flux, red, tid, dt);
+    tile_compute<R, K, BASIS, TX, TY, VAR>(A, lim, (t % ntx) * TX, (t / ntx) * TY, buf, flux, red, tid, dt);
     const int tn = t + 2 * (int)gridDim.x;
     if (tn < ntiles)
       tile_load_async<R, K, BASIS, TX, TY>(A, lim, (tn % ntx) * TX, (tn / ntx) * TY, buf, tid);

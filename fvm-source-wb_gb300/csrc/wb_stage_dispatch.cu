@@ -1,5 +1,5 @@
 // wb_stage_dispatch.cu -- picks the compiled stage kernel for a launch: precision, degree,
-// basis, tile shape, and whether the positivity limiter is needed (wb_stage_instances.h).
+// basis, tile shape, and the variant -- positivity limiter and HLLC flux (wb_stage_instances.h).
 #include <type_traits>
 
 #include "wb_internal.h"
@@ -7,8 +7,8 @@
 
 namespace wb {
 
-#define WB_DECL(P, R, K, BT, B, TX, TY, POS)                                                  \
-  cudaError_t WB_STAGE_INSTANCE_NAME(P, K, BT, TX, TY, POS)(const StageArgs<R> &A,          \
+#define WB_DECL(P, R, K, BT, B, TX, TY, VAR)                                                  \
+  cudaError_t WB_STAGE_INSTANCE_NAME(P, K, BT, TX, TY, VAR)(const StageArgs<R> &A,          \
                                                             cudaStream_t s);
 WB_STAGE_INSTANCES(WB_DECL)
 #undef WB_DECL
@@ -29,11 +29,16 @@ bool wants_positivity(const StageArgs<R> &A, int K) {
 template <typename R>
 cudaError_t dispatch(const StageArgs<R> &A, int K, int basis, int TX, int TY, cudaStream_t s) {
   const int b = K == 0 ? 1 : basis;  // one mode: both bases are the same kernel
-  const int pos = wants_positivity(A, K) ? 1 : 0;
-#define WB_CASE(P, R_, K_, BT, B_, TX_, TY_, POS_)                                            \
+  const int var = (wants_positivity(A, K) ? WB_VAR_POSITIVITY : 0) |
+                  (A.riemann == 1 ? WB_VAR_HLLC : 0);
+  if (var != 0) {  // the variants are compiled for the default tile of the precision
+    TX = std::is_same<R, float>::value ? 32 : 16;
+    TY = 8;
+  }
+#define WB_CASE(P, R_, K_, BT, B_, TX_, TY_, VAR_)                                            \
   if constexpr (std::is_same<R, R_>::value) {                                               \
-    if (K == K_ && b == B_ && TX == TX_ && TY == TY_ && pos == POS_)                        \
-      return WB_STAGE_INSTANCE_NAME(P, K_, BT, TX_, TY_, POS_)(A, s);                       \
+    if (K == K_ && b == B_ && TX == TX_ && TY == TY_ && var == VAR_)                        \
+      return WB_STAGE_INSTANCE_NAME(P, K_, BT, TX_, TY_, VAR_)(A, s);                       \
   }
   WB_STAGE_INSTANCES(WB_CASE)
 #undef WB_CASE
@@ -52,8 +57,9 @@ cudaError_t launch_stage(const StageArgs<double> &A, int K, int basis, int TX, i
 }
 
 bool tile_supported(int precision_fp32, int tx, int ty) {
-#define WB_TILE(P, R_, K_, BT, B_, TX_, TY_, POS_)                                            \
-  if (std::is_same<R_, float>::value == (precision_fp32 != 0) && tx == TX_ && ty == TY_)    \
+#define WB_TILE(P, R_, K_, BT, B_, TX_, TY_, VAR_)                                            \
+  if (VAR_ == 0 && std::is_same<R_, float>::value == (precision_fp32 != 0) && tx == TX_ &&  \
+      ty == TY_)                                                                            \
     return true;
   WB_STAGE_INSTANCES(WB_TILE)
 #undef WB_TILE

@@ -6,11 +6,11 @@
 
 namespace wb {
 
-template <typename R, int K, int BASIS, int TX, int TY, bool POS>
+template <typename R, int K, int BASIS, int TX, int TY, int VAR>
 static cudaError_t launch_stage_kernel(const StageArgs<R> &A, cudaStream_t s) {
   const int lim = A.limiter == 1 && A.lim_y && K >= 1;
   const size_t smem = stage_smem_bytes<R>(K, BASIS, TX, TY, lim);
-  auto kern = k_stage<R, K, BASIS, TX, TY, POS>;
+  auto kern = k_stage<R, K, BASIS, TX, TY, VAR>;
   static int per_sm[2] = {0, 0};  // occupancy per limiter setting, queried once
   if (per_sm[lim] == 0) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -39,10 +39,10 @@ static cudaError_t launch_stage_kernel(const StageArgs<R> &A, cudaStream_t s) {
 }  // namespace wb
 
 // One compiled stage kernel (a line of wb_stage_instances.h) and its launcher.
-#define WB_STAGE_INSTANCE(P, R, K, BT, B, TX, TY, POS)                                      \
+#define WB_STAGE_INSTANCE(P, R, K, BT, B, TX, TY, VAR)                                      \
   namespace wb {                                                                            \
-  cudaError_t WB_STAGE_INSTANCE_NAME(P, K, BT, TX, TY, POS)(const StageArgs<R> &A,          \
+  cudaError_t WB_STAGE_INSTANCE_NAME(P, K, BT, TX, TY, VAR)(const StageArgs<R> &A,          \
                                                             cudaStream_t s) {               \
-    return launch_stage_kernel<R, K, B, TX, TY, (POS != 0)>(A, s);                          \
+    return launch_stage_kernel<R, K, B, TX, TY, VAR>(A, s);                                 \
   }                                                                                         \
   }

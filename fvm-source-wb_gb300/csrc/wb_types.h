@@ -73,6 +73,10 @@ struct Combo {
   R beta, cdt;
 };
 
+// Compile-time variants of the stage kernel (bit mask).
+constexpr int WB_VAR_POSITIVITY = 1;  // Zhang-Shu positivity limiter (limiter 2)
+constexpr int WB_VAR_HLLC = 2;        // HLLC face flux instead of LLF
+
 template <typename R>
 struct StageArgs {
   const R *x;                 // stage input (loaded with halo, limited if lim_y)
@@ -80,6 +84,7 @@ struct StageArgs {
   int nx, ny;
   long long plane;            // elements between (var, mode) planes
   int bc_x, bc_y, llf_speed, limiter, lim_y;  // limiter: 0 off, 1 minmod, 2 positivity
+  int riemann;                // 0 LLF, 1 HLLC (the kernel variant must match)
   int eq_kind;
   R dx, dy, hidx, hidy;       // hidx = 0.5/dx, hidy = 0.5/dy
   R gamma, gm1, igm1, hgam;   // hgam = gamma/(gamma-1)

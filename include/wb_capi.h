@@ -48,6 +48,8 @@ extern "C" {
 #define WB_LLF_REF2D 1      /* lambda = max(|v_n+c|) as compute_llflux of 2d/benchmark_2d_dg.f90 */
 #define WB_PREC_FP64 0      /* "plain": FP64 state, literal F(u_eq+d) - F(u_eq) split */
 #define WB_PREC_FP32 1      /* FP64 equilibrium tables + FP32 perturbation, exact-difference fluxes */
+#define WB_RIEMANN_LLF 0    /* compute_llflux (2d/benchmark_2d_dg.f90:968-988); riemann=1 */
+#define WB_RIEMANN_HLLC 1   /* riemann_hllc (dg_with_source.f90:1318-1374); riemann=2 */
 #define WB_LIMITER_NONE 0
 #define WB_LIMITER_MINMOD 1     /* limiter_type '1OR' (compute_limiter) on the perturbation */
 #define WB_LIMITER_POSITIVITY 2 /* limiter_type 'ONP' (compute_positivity) in delta form */
@@ -70,6 +72,8 @@ typedef struct {
   int32_t integrator;    /* WB_RK2 or WB_RK54 */
   int32_t tile_x, tile_y;/* CTA tile in cells; 0 = tuned default */
   int32_t device;        /* CUDA device ordinal */
+  int32_t riemann;       /* WB_RIEMANN_LLF or WB_RIEMANN_HLLC */
+  int32_t reserved;      /* 0 */
   double gamma;
   double gx, gy;         /* Phi = gx x + gy y */
   double rho0, p0;       /* isothermal reference state */

@@ -25,7 +25,7 @@ class OrcCfg(ctypes.Structure):
         ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("order", ctypes.c_int),
         ("basis", ctypes.c_int), ("bc_x", ctypes.c_int), ("bc_y", ctypes.c_int),
         ("eq_kind", ctypes.c_int), ("llf_speed", ctypes.c_int), ("limiter", ctypes.c_int),
-        ("pad0", ctypes.c_int),
+        ("riemann", ctypes.c_int),
         ("gamma", ctypes.c_double), ("gx", ctypes.c_double), ("gy", ctypes.c_double),
         ("rho0", ctypes.c_double), ("p0", ctypes.c_double), ("kpoly", ctypes.c_double),
         ("lx", ctypes.c_double), ("ly", ctypes.c_double),
@@ -103,7 +103,9 @@ def lib():
         L.orc_uniform.restype = d
         L.orc_uniform.argtypes = [p]
         L.orc_ref2d_compute_update.argtypes = [i, i, i, d, d, d, i, i, i, d, d, i, p, p]
-        L.orc_dg1d_update_exact_delta.argtypes = [i, i, d, d, i, p, p]
+        L.orc_dg1d_update_exact_delta.argtypes = [i, i, d, d, i, i, p, p]
+        L.orc_ref_riemann_hllc.argtypes = [d, p, p, p]
+        L.orc_num_flux.argtypes = [p, p, p, i, p]
         L.orc_fv1d_rhs.argtypes = [p, p, p]
         L.orc_fv1d_run.restype = d
         L.orc_fv1d_run.argtypes = [p, p, d, i, p]
@@ -119,13 +121,14 @@ def _ptr(a):
 def make_cfg(nx=16, ny=16, order=1, basis=BASIS_P, bc_x=BC_COPY, bc_y=BC_COPY,
              eq_kind=EQ_ISOTHERMAL, llf_speed=LLF_MAXABS, limiter=0, gamma=1.4, gx=1.0, gy=1.0,
              rho0=1.0, p0=1.0, kpoly=1.0, lx=1.0, ly=1.0, lim_norm=3.0, lim_M=0.0,
-             lim_tol=1e-6, cfl=0.3, pos_eps=1e-10):
+             lim_tol=1e-6, cfl=0.3, pos_eps=1e-10, riemann=0):
     c = OrcCfg()
     c.nx, c.ny, c.order, c.basis = nx, ny, order, basis
     c.bc_x, c.bc_y, c.eq_kind, c.llf_speed, c.limiter = bc_x, bc_y, eq_kind, llf_speed, limiter
     c.gamma, c.gx, c.gy, c.rho0, c.p0, c.kpoly = gamma, gx, gy, rho0, p0, kpoly
     c.lx, c.ly, c.lim_norm, c.lim_M, c.lim_tol, c.cfl = lx, ly, lim_norm, lim_M, lim_tol, cfl
     c.pos_eps = pos_eps
+    c.riemann = riemann
     return c
 
 
@@ -303,12 +306,31 @@ def ref2d_compute_update(u_f, nx, ny, m, gamma=1.4, lx=1.0, ly=1.0, flux_bug=0, 
     return out
 
 
-def dg1d_update_exact_delta(du_f, nx, n, gamma=1.4, lx=1.0, half_source=1):
-    """du_f: Fortran-ordered array (3, n, nx)."""
+def dg1d_update_exact_delta(du_f, nx, n, gamma=1.4, lx=1.0, half_source=1, riemann=1):
+    """du_f: Fortran-ordered array (3, n, nx); riemann: 1 riemann_llf, 2 riemann_hllc."""
     du_f = np.asfortranarray(du_f, dtype=np.float64)
     out = np.zeros_like(du_f, order="F")
-    lib().orc_dg1d_update_exact_delta(nx, n, gamma, lx, half_source, _ptr(du_f), _ptr(out))
+    lib().orc_dg1d_update_exact_delta(nx, n, gamma, lx, half_source, riemann, _ptr(du_f),
+                                      _ptr(out))
     return out
+
+
+def ref_riemann_hllc(ul, ur, gamma=1.4):
+    """riemann_hllc of dg_with_source.f90 (1D states rho, rho u, E)."""
+    ul = np.ascontiguousarray(ul, dtype=np.float64)
+    ur = np.ascontiguousarray(ur, dtype=np.float64)
+    f = np.zeros(3)
+    lib().orc_ref_riemann_hllc(gamma, _ptr(ul), _ptr(ur), _ptr(f))
+    return f
+
+
+def num_flux(cfg, uL, uR, direction):
+    """The composed scheme's numerical flux (cfg.riemann) of two 2D states."""
+    uL = np.ascontiguousarray(uL, dtype=np.float64)
+    uR = np.ascontiguousarray(uR, dtype=np.float64)
+    f = np.zeros(4)
+    lib().orc_num_flux(ctypes.byref(cfg), _ptr(uL), _ptr(uR), int(direction), _ptr(f))
+    return f
 
 
 def make_fv1d(nx=256, bc=1, limiter=1, eq_kind=EQ_ISOTHERMAL, gamma=1.4, g=1.0, rho0=1.0,

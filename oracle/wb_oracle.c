@@ -244,6 +244,53 @@ static inline void llf(const orc_cfg *c, const double *uL, const double *uR, int
   for (int v = 0; v < NV; ++v) fh[v] = 0.5 * (fR[v] + fL[v]) + 0.5 * cmax * (uL[v] - uR[v]);
 }
 
+/* HLLC (riemann = 2 of dg_with_source.f90; riemann_hllc :1318-1374) for 2D states, the
+ * transverse velocity carried by the contact.  Davis wave speeds S_L = min(v_L, v_R) -
+ * max(c_L, c_R), S_R = max(v_L, v_R) + max(c_L, c_R) (:1332-1333), contact speed from the
+ * Lagrangian speeds D_L = rho_L (v_L - S_L), D_R = rho_R (S_R - v_R) (:1335-1338), sampled
+ * at x/t = 0 in the order of :1346-1366.  The star fluxes are written F_K + S_K (U*_K - U_K)
+ * with U*_K - U_K = (S* - v_K)/(S_K - S*) [rho_K, rho_K S_K, rho_K vt_K,
+ * E_K + p_K + rho_K S* (S_K - v_K)], which equals riemann_hllc's F(U*_K) in exact arithmetic
+ * and gives F(u) bit for bit when u_L = u_R at rest (S* = v_K = 0). */
+static inline void hllc(const orc_cfg *c, const double *uL, const double *uR, int dir,
+                        double *fh) {
+  double wL[NV], wR[NV], fL[NV], fR[NV];
+  prim(c->gamma, uL, wL);
+  prim(c->gamma, uR, wR);
+  flux_dir(uL, wL, dir, fL);
+  flux_dir(uR, wR, dir, fR);
+  const double cL = sound(c->gamma, wL), cR = sound(c->gamma, wR);
+  const double vL = wL[1 + dir], vR = wR[1 + dir];
+  const double SL = fmin(vL, vR) - fmax(cL, cR), SR = fmax(vL, vR) + fmax(cL, cR);
+  const double DL = wL[0] * (vL - SL), DR = wR[0] * (SR - vR);
+  const double Ss = (DR * vR + DL * vL + (wL[3] - wR[3])) / (DL + DR);
+  const double *u, *w, *f;
+  double SK;
+  if (SL > 0.0) {
+    for (int v = 0; v < NV; ++v) fh[v] = fL[v];
+    return;
+  } else if (Ss > 0.0) {
+    u = uL; w = wL; f = fL; SK = SL;
+  } else if (SR > 0.0) {
+    u = uR; w = wR; f = fR; SK = SR;
+  } else {
+    for (int v = 0; v < NV; ++v) fh[v] = fR[v];
+    return;
+  }
+  const double vK = w[1 + dir], q = SK * ((Ss - vK) / (SK - Ss));
+  double d[NV];
+  d[0] = w[0];
+  d[1 + dir] = w[0] * SK;
+  d[2 - dir] = w[0] * w[2 - dir];
+  d[3] = (u[3] + w[3]) + w[0] * Ss * (SK - vK);
+  for (int v = 0; v < NV; ++v) fh[v] = f[v] + q * d[v];
+}
+
+void orc_num_flux(const orc_cfg *c, const double *uL, const double *uR, int dir, double *f) {
+  if (c->riemann == ORC_RIEMANN_HLLC) hllc(c, uL, uR, dir, f);
+  else llf(c, uL, uR, dir, f);
+}
+
 /* BC index map, 2d/benchmark_2d_dg.f90:777-824 (bc=1 periodic, bc=2,3 copy) */
 static inline int bcmap(int i, int n, int bc) {
   if (i < 0) return bc == ORC_BC_PERIODIC ? i + n : 0;
@@ -423,7 +470,7 @@ void orc_rhs(const orc_cfg *c, const double *delta, double *dudt) {
           uL[v] = ue[v] + dL[v];
           uR[v] = ue[v] + dR[v];
         }
-        llf(c, uL, uR, 0, fh);
+        orc_num_flux(c, uL, uR, 0, fh);
         prim(g, ue, we);
         flux_dir(ue, we, 0, fe);
         for (int v = 0; v < NV; ++v)
@@ -449,7 +496,7 @@ void orc_rhs(const orc_cfg *c, const double *delta, double *dudt) {
           uB[v] = ue[v] + dB[v];
           uT[v] = ue[v] + dT[v];
         }
-        llf(c, uB, uT, 1, fh);
+        orc_num_flux(c, uB, uT, 1, fh);
         prim(g, ue, we);
         flux_dir(ue, we, 1, fe);
         for (int v = 0; v < NV; ++v)
@@ -1118,6 +1165,38 @@ static inline void llf1(double g, const double *ul, const double *ur, double *f)
   flux1(g, ur, fr);
   for (int v = 0; v < 3; ++v) f[v] = 0.5 * (fr[v] + fl[v]) - 0.5 * cmax * (ur[v] - ul[v]);
 }
+/* riemann_hllc, dg_with_source.f90:1318-1374: acoustic star state from the Lagrangian
+ * sound speeds, sampled at x/t = 0, flux of the sampled state */
+void orc_ref_riemann_hllc(double g, const double *ul, const double *ur, double *fg) {
+  double wl[3], wr[3], wst[3], wstl[3], wstr[3], ustl[3], ustr[3], wgd[3], ugd[3];
+  prim1(g, ul, wl);
+  prim1(g, ur, wr);
+  const double cl = sqrt(g * fmax(wl[2], 1e-10) / fmax(wl[0], 1e-10));
+  const double cr = sqrt(g * fmax(wr[2], 1e-10) / fmax(wr[0], 1e-10));
+  const double SL = fmin(wl[1], wr[1]) - fmax(cl, cr);
+  const double SR = fmax(wl[1], wr[1]) + fmax(cl, cr);
+  const double DL = wl[0] * (wl[1] - SL);
+  const double DR = wr[0] * (SR - wr[1]);
+  wst[1] = (DR * wr[1] + DL * wl[1] + (wl[2] - wr[2])) / (DL + DR);
+  wst[2] = (DR * wl[2] + DL * wr[2] + DL * DR * (wl[1] - wr[1])) / (DL + DR);
+  wstl[0] = wl[0] * (SL - wl[1]) / (SL - wst[1]);
+  ustl[2] = ((SL - wl[1]) * ul[2] - wl[2] * wl[1] + wst[2] * wst[1]) / (SL - wst[1]);
+  wstr[0] = wr[0] * (SR - wr[1]) / (SR - wst[1]);
+  ustr[2] = ((SR - wr[1]) * ur[2] - wr[2] * wr[1] + wst[2] * wst[1]) / (SR - wst[1]);
+  if (SL > 0.0) {
+    wgd[0] = wl[0]; wgd[1] = wl[1]; wgd[2] = wl[2]; ugd[2] = ul[2];
+  } else if (wst[1] > 0.0) {
+    wgd[0] = wstl[0]; wgd[1] = wst[1]; wgd[2] = wst[2]; ugd[2] = ustl[2];
+  } else if (SR > 0.0) {
+    wgd[0] = wstr[0]; wgd[1] = wst[1]; wgd[2] = wst[2]; ugd[2] = ustr[2];
+  } else {
+    wgd[0] = wr[0]; wgd[1] = wr[1]; wgd[2] = wr[2]; ugd[2] = ur[2];
+  }
+  fg[0] = wgd[0] * wgd[1];
+  fg[1] = wgd[0] * wgd[1] * wgd[1] + wgd[2];
+  fg[2] = wgd[1] * (ugd[2] + wgd[2]);
+}
+
 static inline void source1(double g, const double *u, double *s) {
   double w[3];
   prim1(g, u, w);
@@ -1128,13 +1207,13 @@ static inline void source1(double g, const double *u, double *s) {
 
 /*
  * compute_update_exact_delta, dg_with_source.f90:1749-2031, with riemann_llf
- * (riemann=1), equilibrium rho = p = exp(-x) (get_eq_solution :1031-1048) and the
+ * (riemann=1) or riemann_hllc (riemann=2, :1909-1917), equilibrium rho = p = exp(-x) (get_eq_solution :1031-1048) and the
  * sqrt(2n+1) basis of 2d/legendre.f90 (for which the 1/dx and 0.5 factors of
  * :1998-2025 are the consistent ones).  Out-of-range faces wrap periodically; the
  * two end cells are frozen (:2028-2029) so they never reach the result.
  */
 void orc_dg1d_update_exact_delta(int nx, int n, double g, double lx, int half_source,
-                                 const double *du, double *dudt) {
+                                 int riemann, const double *du, double *dudt) {
 #define D1(v, i, c) ((v) + 3 * ((i) + (size_t)n * (c)))
   double xq[NQMAX], wq[NQMAX];
   orc_gl_quadrature(n, xq, wq);
@@ -1194,7 +1273,8 @@ void orc_dg1d_update_exact_delta(int nx, int n, double g, double lx, int half_so
   }
   for (int f = 0; f <= nx; ++f) {
     int il = f - 1 < 0 ? nx - 1 : f - 1, ir = f > nx - 1 ? 0 : f;
-    llf1(g, ur + 3 * il, ul + 3 * ir, fface + 3 * f);
+    if (riemann == 2) orc_ref_riemann_hllc(g, ur + 3 * il, ul + 3 * ir, fface + 3 * f);
+    else llf1(g, ur + 3 * il, ul + 3 * ir, fface + 3 * f);
   }
   for (int c = 0; c < nx; ++c)
     for (int i = 0; i < n; ++i)

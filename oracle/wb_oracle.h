@@ -27,6 +27,7 @@ enum { ORC_BASIS_Q = 0, ORC_BASIS_P = 1 };
 enum { ORC_BC_PERIODIC = 0, ORC_BC_COPY = 1 };
 enum { ORC_EQ_NONE = 0, ORC_EQ_ISOTHERMAL = 1, ORC_EQ_POLYTROPE = 2 };
 enum { ORC_LLF_MAXABS = 0, ORC_LLF_REF2D = 1 };
+enum { ORC_RIEMANN_LLF = 0, ORC_RIEMANN_HLLC = 1 };
 
 typedef struct {
   int nx, ny;        /* cells per direction */
@@ -37,7 +38,7 @@ typedef struct {
   int llf_speed;     /* ORC_LLF_* wave-speed estimate */
   int limiter;       /* 0 off, 1 minmod moment limiter on the perturbation,
                         2 Zhang-Shu positivity limiter (in delta form) */
-  int pad0;
+  int riemann;       /* ORC_RIEMANN_LLF or ORC_RIEMANN_HLLC */
   double gamma;
   double gx, gy;     /* constant gravity: Phi = gx*x + gy*y */
   double rho0, p0;   /* isothermal: rho = rho0*exp(-(rho0/p0)*Phi), p = p0*exp(-(rho0/p0)*Phi) */
@@ -129,7 +130,13 @@ void orc_ref2d_compute_update(int nx, int ny, int m, double gamma, double lx, do
  * end-cell freeze of :2028-2029.  half_source=1 keeps the 0.5 on the source
  * projection (as :1998-2006 do).  Layout u(nvar=3, n, nx) column-major. */
 void orc_dg1d_update_exact_delta(int nx, int n, double gamma, double lx, int half_source,
-                                 const double *delta_u, double *dudt);
+                                 int riemann, const double *delta_u, double *dudt);
+/* (riemann above is the reference's own switch: 1 riemann_llf, 2 riemann_hllc) */
+/* riemann_hllc, dg_with_source.f90:1318-1374 (1D, u = (rho, rho u, E)), literal */
+void orc_ref_riemann_hllc(double gamma, const double *ul, const double *ur, double *f);
+/* The composed scheme's numerical flux of 2D states in direction dir (0 x, 1 y):
+ * LLF or HLLC as cfg->riemann says */
+void orc_num_flux(const orc_cfg *c, const double *uL, const double *uR, int dir, double *f);
 
 /* ---- 1D well-balanced FV (benchmark_1d.f90:263-377) with minmod MUSCL on delta ---- */
 typedef struct {

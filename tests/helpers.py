@@ -6,13 +6,13 @@ import pyoracle as O
 
 _CFG_KEYS = ("nx", "ny", "order", "basis", "bc_x", "bc_y", "eq_kind", "llf_speed", "limiter",
              "gamma", "gx", "gy", "rho0", "p0", "kpoly", "lx", "ly", "lim_norm", "lim_M",
-             "lim_tol", "cfl", "pos_eps")
+             "lim_tol", "cfl", "pos_eps", "riemann")
 
 
 def base_cfg(**kw):
     c = dict(nx=12, ny=10, order=1, basis=1, bc_x=1, bc_y=1, eq_kind=1, llf_speed=0, limiter=0,
              gamma=1.4, gx=1.0, gy=1.0, rho0=1.0, p0=1.0, kpoly=1.0, lx=1.0, ly=1.0,
-             lim_norm=3.0, lim_M=0.0, lim_tol=1e-6, cfl=0.3, pos_eps=1e-10)
+             lim_norm=3.0, lim_M=0.0, lim_tol=1e-6, cfl=0.3, pos_eps=1e-10, riemann=0)
     c.update(kw)
     return c
 

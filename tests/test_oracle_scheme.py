@@ -9,8 +9,10 @@ from helpers import base_cfg, orc_cfg, random_delta
 
 @pytest.mark.parametrize("order,basis", [(0, 0), (1, 0), (1, 1), (2, 0), (2, 1)])
 @pytest.mark.parametrize("eq_kind", [1, 2])
-def test_zero_perturbation_exact(orc, order, basis, eq_kind):
-    c = base_cfg(order=order, basis=basis, eq_kind=eq_kind, gx=0.4, gy=1.0, limiter=1)
+@pytest.mark.parametrize("riemann", [0, 1])
+def test_zero_perturbation_exact(orc, order, basis, eq_kind, riemann):
+    c = base_cfg(order=order, basis=basis, eq_kind=eq_kind, gx=0.4, gy=1.0, limiter=1,
+                 riemann=riemann)
     oc = orc_cfg(c)
     z = np.zeros((4, orc.nb(oc), c["ny"], c["nx"]))
     assert np.all(orc.rhs(oc, z) == 0.0)
@@ -56,11 +58,13 @@ def test_reference_flux_type_defect_reproduced(orc):
 
 
 @pytest.mark.parametrize("order", [0, 1, 2])
-def test_matches_literal_reference_1d_wb_operator(orc, order):
+@pytest.mark.parametrize("riemann", [0, 1])
+def test_matches_literal_reference_1d_wb_operator(orc, order, riemann):
     """y-uniform data reduce the 2D well-balanced operator to the 1D
     compute_update_exact_delta of dg_with_source.f90:1749-2031 (interior cells)."""
     n, nx = order + 1, 10
-    c = base_cfg(nx=nx, ny=1, order=order, basis=0, eq_kind=1, gx=1.0, gy=0.0, bc_x=0, bc_y=0)
+    c = base_cfg(nx=nx, ny=1, order=order, basis=0, eq_kind=1, gx=1.0, gy=0.0, bc_x=0, bc_y=0,
+                 riemann=riemann)
     oc = orc_cfg(c)
     a, b = orc.modes(order, 0)
     rng = np.random.default_rng(1)
@@ -72,7 +76,7 @@ def test_matches_literal_reference_1d_wb_operator(orc, order):
         d[0, mm, 0], d[1, mm, 0], d[3, mm, 0] = vals
         d1[:, k, :] = vals
     r2 = orc.rhs(oc, d)
-    r1 = orc.dg1d_update_exact_delta(d1, nx, n)
+    r1 = orc.dg1d_update_exact_delta(d1, nx, n, riemann=riemann + 1)
     for k in range(n):
         mm = [i for i in range(len(a)) if a[i] == k and b[i] == 0][0]
         for v2, v1 in ((0, 0), (1, 1), (3, 2)):
@@ -127,3 +131,52 @@ def test_fv1d_equilibrium_and_perturbation(orc):
     assert n > 50
     # the pressure pulse splits and travels; its energy perturbation stays O(amp)
     assert 1e-5 < np.max(np.abs(d[:, 2])) < 3e-3
+
+
+def _state2d(rho, vx, vy, p, gamma=1.4):
+    return np.array([rho, rho * vx, rho * vy, p / (gamma - 1) + 0.5 * rho * (vx * vx + vy * vy)])
+
+
+@pytest.mark.parametrize("case", range(6))
+@pytest.mark.parametrize("direction", [0, 1])
+def test_hllc_matches_reference_riemann_hllc(orc, case, direction):
+    """The composed scheme's HLLC in one direction, no transverse velocity, equals
+    riemann_hllc of dg_with_source.f90 on the 1D states: subsonic both ways,
+    supersonic both ways, strong pressure jump."""
+    left, right = [((1.0, 0.1, 1.0), (0.8, -0.2, 0.7)), ((1.0, -0.3, 1.0), (0.9, -0.4, 1.2)),
+                   ((1.0, 3.0, 1.0), (0.5, 2.5, 0.4)), ((0.7, -3.0, 0.6), (1.0, -2.8, 1.0)),
+                   ((1.0, 0.0, 1000.0), (1.0, 0.0, 0.01)), ((0.125, 0.0, 0.1), (1.0, 0.0, 1.0))][case]
+    oc = orc_cfg(base_cfg(riemann=1))
+    g = 1.4
+    vl = (left[1], 0.0) if direction == 0 else (0.0, left[1])
+    vr = (right[1], 0.0) if direction == 0 else (0.0, right[1])
+    f2 = orc.num_flux(oc, _state2d(left[0], *vl, left[2]), _state2d(right[0], *vr, right[2]),
+                      direction)
+    u1l = np.array([left[0], left[0] * left[1], left[2] / (g - 1) + 0.5 * left[0] * left[1] ** 2])
+    u1r = np.array([right[0], right[0] * right[1], right[2] / (g - 1) + 0.5 * right[0] * right[1] ** 2])
+    f1 = orc.ref_riemann_hllc(u1l, u1r)
+    n = 1 + direction
+    got = np.array([f2[0], f2[n], f2[3]])
+    np.testing.assert_allclose(got, f1, rtol=1e-13, atol=1e-13 * np.max(np.abs(f1)))
+    assert f2[3 - n] == 0.0  # no transverse velocity, no transverse momentum flux
+
+
+@pytest.mark.parametrize("riemann", [0, 1])
+def test_numerical_flux_consistent(orc, riemann):
+    """F_hat(u, u) = F(u): bit for bit at rest, to round-off when moving."""
+    oc = orc_cfg(base_cfg(riemann=riemann))
+    g = 1.4
+    rest = _state2d(0.9, 0.0, 0.0, 0.7)
+    for d in (0, 1):
+        f = orc.num_flux(oc, rest, rest, d)
+        exp = np.zeros(4)
+        exp[1 + d] = 0.7
+        np.testing.assert_array_equal(f, exp)
+    mov = _state2d(0.9, 0.3, -0.2, 0.7)
+    for d in (0, 1):
+        f = orc.num_flux(oc, mov, mov, d)
+        v = mov[1 + d] / mov[0]
+        p = 0.7
+        exp = np.array([mov[1 + d], mov[1] * v, mov[2] * v, v * (mov[3] + p)])
+        exp[1 + d] += p
+        np.testing.assert_allclose(f, exp, rtol=1e-14, atol=1e-15)
