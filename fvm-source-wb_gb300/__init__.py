@@ -27,6 +27,7 @@ PREC_FP64, PREC_FP32 = 0, 1
 RK2, RK54 = 0, 1
 LIMITER_NONE, LIMITER_MINMOD, LIMITER_POSITIVITY = 0, 1, 2
 RIEMANN_LLF, RIEMANN_HLLC = 0, 1
+SCHEME_EQL, SCHEME_WB1 = 0, 1
 LAYOUT_SOA, LAYOUT_FORTRAN = 0, 1
 
 
@@ -54,7 +55,7 @@ class WbPerturbation(ctypes.Structure):
 
 
 class Wb1dConfig(ctypes.Structure):
-    _fields_ = [(n, ctypes.c_int32) for n in ("nx", "bc", "limiter", "eq_kind", "device", "pad")] + [
+    _fields_ = [(n, ctypes.c_int32) for n in ("nx", "bc", "limiter", "eq_kind", "device", "scheme")] + [
         (n, ctypes.c_double) for n in ("gamma", "g", "rho0", "p0", "kpoly", "lx", "cfl")]
 
 
@@ -547,10 +548,13 @@ class Solver1D:
     """
 
     def __init__(self, nx=256, bc=BC_COPY, limiter=1, eq_kind=EQ_ISOTHERMAL, gamma=1.4, g=1.0,
-                 rho0=1.0, p0=1.0, kpoly=1.0, lx=1.0, cfl=0.4, device=0):
+                 rho0=1.0, p0=1.0, kpoly=1.0, lx=1.0, cfl=0.4, device=0, scheme=0):
+        """scheme: SCHEME_EQL ('EQL', equilibrium + perturbation faces) or SCHEME_WB1
+        ('WB1', hydrostatic reconstruction of compute_update_sr)."""
         L = lib()
         c = Wb1dConfig()
         c.nx, c.bc, c.limiter, c.eq_kind, c.device = nx, bc, limiter, eq_kind, device
+        c.scheme = scheme
         c.gamma, c.g, c.rho0, c.p0, c.kpoly, c.lx, c.cfl = gamma, g, rho0, p0, kpoly, lx, cfl
         self.cfg = c
         self._c = ctypes.c_void_p()

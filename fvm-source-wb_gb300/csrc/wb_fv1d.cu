@@ -1,5 +1,6 @@
 // wb_fv1d.cu -- 1D well-balanced finite-volume step (the fvm.f90 / benchmark_1d.f90 path)
-// on the device, FP64.
+// on the device, FP64.  Two schemes: 'EQL' (below) and the hydrostatic reconstruction
+// 'WB1' (rhs_wb1).
 //
 // Scheme (compute_update 'EQL', benchmark_1d.f90:263-377): face states are the
 // equilibrium at the face plus the perturbation of the adjacent cell, reconstructed
@@ -21,7 +22,7 @@
 namespace {
 
 struct Fv1dArgs {
-  int nx, bc, limiter, max_steps, rhs_only;
+  int nx, bc, limiter, max_steps, rhs_only, scheme;
   double dx, gamma, g, cfl, tend;
   double *d, *w1, *fh, *L;       // state, stage state, face fluxes [(nx+1)*3], rhs [nx*3]
   const double *re, *pe;         // equilibrium at centres
@@ -66,8 +67,68 @@ __device__ __forceinline__ double slope(const Fv1dArgs &A, const double *d, int 
   return mm3(dp, dm, dm);
 }
 
+// 'WB1' face states of cell i (compute_update_sr, benchmark_1d.f90:553-747): the cell's
+// specific enthalpy h = p/rho (1 + 1/(gamma-1)) and K = p/rho^gamma (default-real floor
+// 1e-5, :611,619) carried to its faces along h + Phi = const (Phi = g x, :615-616), with
+// the cell velocity (:631-635).  w receives the cell's primitive state.
+__device__ void wb1_face_states(const Fv1dArgs &A, const double *d, int i, double *uL,
+                                double *uR, double &pL, double &pR, double *w) {
+  const double g = A.gamma, fl = (double)1e-5f;
+  const double u[3] = {A.re[i] + d[3 * i], d[3 * i + 1], A.pe[i] / (g - 1.0) + d[3 * i + 2]};
+  prim1(g, u, w);
+  const double h = fmax(w[2], fl) / fmax(fl, w[0]) * (1 + 1. / (g - 1));
+  const double xc = ((double)i + 0.5) * A.dx, xl = (double)i * A.dx, xr = (double)(i + 1) * A.dx;
+  const double h0l = h + A.g * xc - A.g * xl, h0r = h + A.g * xc - A.g * xr;
+  const double K = fmax(fl, w[2]) / pow(fmax(fl, w[0]), g);
+  const double rl = pow((1. / K) * (g - 1) / g * h0l, 1 / (g - 1));
+  const double rr = pow((1. / K) * (g - 1) / g * h0r, 1 / (g - 1));
+  pL = pow(1. / K, 1 / (g - 1)) * pow((g - 1) / g * h0l, g / (g - 1));
+  pR = pow(1. / K, 1 / (g - 1)) * pow((g - 1) / g * h0r, g / (g - 1));
+  uL[0] = rl;
+  uL[1] = rl * w[1];
+  uL[2] = pL / (g - 1.0) + 0.5 * rl * w[1] * w[1];
+  uR[0] = rr;
+  uR[1] = rr * w[1];
+  uR[2] = pR / (g - 1.0) + 0.5 * rr * w[1] * w[1];
+}
+
+// 'WB1' L(d): LLF of the adjacent face states on the interior faces (:642-666), source
+// (0, (p_right - p_left)/dx, -rho v g (x+ - x-)/(2 dx)) (get_source_rg :409-434), the end
+// cells take their neighbour's update (:741-742).
+__device__ void rhs_wb1(const Fv1dArgs &A, const double *d) {
+  const int nx = A.nx;
+  for (int f = 1 + threadIdx.x; f < nx; f += blockDim.x) {
+    double aL[3], aR[3], bL[3], bR[3], p1, p2, p3, p4, w[3], fa[3], fb[3];
+    wb1_face_states(A, d, f - 1, aL, aR, p1, p2, w);
+    wb1_face_states(A, d, f, bL, bR, p3, p4, w);
+    flux1(A.gamma, aR, fa);
+    flux1(A.gamma, bL, fb);
+    const double cmax = fmax(speed1(A.gamma, aR), speed1(A.gamma, bL));
+    for (int v = 0; v < 3; ++v) A.fh[3 * f + v] = 0.5 * (fb[v] + fa[v]) - 0.5 * cmax * (bL[v] - aR[v]);
+  }
+  __syncthreads();
+  for (int i = 1 + threadIdx.x; i < nx - 1; i += blockDim.x) {
+    double uL[3], uR[3], pL, pR, w[3];
+    wb1_face_states(A, d, i, uL, uR, pL, pR, w);
+    const double xm = ((double)(i - 1) + 0.5) * A.dx, xp = ((double)(i + 1) + 0.5) * A.dx;
+    const double s[3] = {0.0, (pR - pL) / A.dx, -w[0] * w[1] * A.g * (xp - xm) / (2 * A.dx)};
+    for (int v = 0; v < 3; ++v) A.L[3 * i + v] = -(A.fh[3 * (i + 1) + v] - A.fh[3 * i + v]) / A.dx + s[v];
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    const int v = threadIdx.x;
+    A.L[v] = A.L[3 + v];
+    A.L[3 * (nx - 1) + v] = A.L[3 * (nx - 2) + v];
+  }
+  __syncthreads();
+}
+
 // L(d) into A.L; face fluxes staged in A.fh.  Called by all threads of the CTA.
 __device__ void rhs(const Fv1dArgs &A, const double *d) {
+  if (A.scheme == WB1D_WB1) {
+    rhs_wb1(A, d);
+    return;
+  }
   const int nx = A.nx;
   const double igm1 = 1.0 / (A.gamma - 1.0);
   for (int f = threadIdx.x; f <= nx; f += blockDim.x) {
@@ -168,6 +229,7 @@ Fv1dArgs args1(wb1d_ctx *c) {
   A.nx = c->cfg.nx;
   A.bc = c->cfg.bc;
   A.limiter = c->cfg.limiter;
+  A.scheme = c->cfg.scheme;
   A.dx = c->cfg.lx / (double)c->cfg.nx;
   A.gamma = c->cfg.gamma;
   A.g = c->cfg.g;
@@ -214,6 +276,9 @@ int wb1d_create(const wb1d_config *cfg, wb1d_ctx **out) {
   *out = c;
   if (cfg->nx < 2 || cfg->nx > (1 << 24)) return e1(c, WB_ERR_CONFIG, "nx must be in [2, 2^24]");
   if (cfg->bc != WB_BC_PERIODIC && cfg->bc != WB_BC_COPY) return e1(c, WB_ERR_CONFIG, "bad bc");
+  if (cfg->scheme != WB1D_EQL && cfg->scheme != WB1D_WB1)
+    return e1(c, WB_ERR_CONFIG, "scheme must be WB1D_EQL or WB1D_WB1");
+  if (cfg->scheme == WB1D_WB1 && cfg->nx < 3) return e1(c, WB_ERR_CONFIG, "'WB1' needs nx >= 3");
   if (cfg->eq_kind != WB_EQ_ISOTHERMAL && cfg->eq_kind != WB_EQ_POLYTROPE)
     return e1(c, WB_ERR_CONFIG, "eq_kind must be isothermal or polytrope");
   if (!(cfg->gamma > 1.0) || !(cfg->lx > 0.0) || !(cfg->cfl > 0.0))

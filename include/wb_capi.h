@@ -230,10 +230,12 @@ typedef struct {
   int32_t limiter;       /* 0 first order, 1 minmod MUSCL on the perturbation */
   int32_t eq_kind;       /* WB_EQ_ISOTHERMAL or WB_EQ_POLYTROPE */
   int32_t device;
-  int32_t pad;
+  int32_t scheme;        /* WB1D_EQL or WB1D_WB1 */
   double gamma, g, rho0, p0, kpoly, lx, cfl;
 } wb1d_config;
-/* compute_update 'EQL' + evolve of benchmark_1d.f90:200-377 on the device */
+#define WB1D_EQL 0  /* compute_update 'EQL' (benchmark_1d.f90:263-377): equilibrium + delta faces */
+#define WB1D_WB1 1  /* compute_update_sr 'WB1' (benchmark_1d.f90:553-747): hydrostatic reconstruction */
+/* compute_update ('EQL' or 'WB1') + evolve of benchmark_1d.f90:200-377 on the device */
 int wb1d_create(const wb1d_config *cfg, wb1d_ctx **out);
 int wb1d_destroy(wb1d_ctx *c);
 const char *wb1d_last_error(const wb1d_ctx *c);

@@ -48,7 +48,7 @@ class OrcIC(ctypes.Structure):
 class OrcFV1D(ctypes.Structure):
     _fields_ = [
         ("nx", ctypes.c_int), ("bc", ctypes.c_int), ("limiter", ctypes.c_int),
-        ("eq_kind", ctypes.c_int),
+        ("eq_kind", ctypes.c_int), ("scheme", ctypes.c_int), ("pad0", ctypes.c_int),
         ("gamma", ctypes.c_double), ("g", ctypes.c_double), ("rho0", ctypes.c_double),
         ("p0", ctypes.c_double), ("kpoly", ctypes.c_double), ("lx", ctypes.c_double),
         ("cfl", ctypes.c_double),
@@ -334,9 +334,9 @@ def num_flux(cfg, uL, uR, direction):
 
 
 def make_fv1d(nx=256, bc=1, limiter=1, eq_kind=EQ_ISOTHERMAL, gamma=1.4, g=1.0, rho0=1.0,
-              p0=1.0, kpoly=1.0, lx=1.0, cfl=0.4):
+              p0=1.0, kpoly=1.0, lx=1.0, cfl=0.4, scheme=0):
     c = OrcFV1D()
-    c.nx, c.bc, c.limiter, c.eq_kind = nx, bc, limiter, eq_kind
+    c.nx, c.bc, c.limiter, c.eq_kind, c.scheme = nx, bc, limiter, eq_kind, scheme
     c.gamma, c.g, c.rho0, c.p0, c.kpoly, c.lx, c.cfl = gamma, g, rho0, p0, kpoly, lx, cfl
     return c
 

@@ -1339,7 +1339,76 @@ static inline double fv_speed(double g, const double *u) {
  * (u_eq(ghost) + delta(edge)).  Differences are formed per face and per cell so a
  * zero perturbation gives an exactly zero update.
  */
+/*
+ * 'WB1' update, compute_update_sr (benchmark_1d.f90:553-747), on the full state
+ * u_i = u_eq(x_i) + delta_i: per cell the specific enthalpy h = p/rho (1 + 1/(gamma-1))
+ * and K = p / rho^gamma, both with the default-real floor 1e-5 (:611,619); h moved to the
+ * faces along h + Phi = const (:615-616, Phi = g x); face states of the cell's own K
+ * with the cell velocity (:631-635); LLF of the adjacent face states on the interior
+ * faces (:642-666, compute_llflux :438-451); source (0, (p_right - p_left)/dx,
+ * -rho v g (x+ - x-)/(2 dx)) (get_source_rg :409-434); the two end cells take their
+ * neighbour's update (:741-742).  The reference's 1/dx is boxlen/dx and its source
+ * spacing 1/nx, which agree with dx for its boxlen = 1; dx is used here.
+ */
+static void wb1_face_states(const orc_fv1d_cfg *c, const double *d, const double *re,
+                            const double *pe, int i, double dx, double *uL, double *uR,
+                            double *pL, double *pR, double *w) {
+  const double g = c->gamma, fl = (double)1e-5f;
+  double u[3] = {re[i] + d[3 * i], d[3 * i + 1], pe[i] / (g - 1.0) + d[3 * i + 2]};
+  fv_prim(g, u, w);
+  const double h = fmax(w[2], fl) / fmax(fl, w[0]) * (1 + 1. / (g - 1));
+  const double xc = ((double)i + 0.5) * dx, xl = (double)i * dx, xr = (double)(i + 1) * dx;
+  const double h0l = h + c->g * xc - c->g * xl, h0r = h + c->g * xc - c->g * xr;
+  const double K = fmax(fl, w[2]) / pow(fmax(fl, w[0]), g);
+  const double rl = pow((1. / K) * (g - 1) / g * h0l, 1 / (g - 1));
+  const double rr = pow((1. / K) * (g - 1) / g * h0r, 1 / (g - 1));
+  *pL = pow(1. / K, 1 / (g - 1)) * pow((g - 1) / g * h0l, g / (g - 1));
+  *pR = pow(1. / K, 1 / (g - 1)) * pow((g - 1) / g * h0r, g / (g - 1));
+  uL[0] = rl;
+  uL[1] = rl * w[1];
+  uL[2] = *pL / (g - 1.0) + 0.5 * rl * w[1] * w[1];
+  uR[0] = rr;
+  uR[1] = rr * w[1];
+  uR[2] = *pR / (g - 1.0) + 0.5 * rr * w[1] * w[1];
+}
+
+static void wb1_rhs(const orc_fv1d_cfg *c, const double *d, double *dudt) {
+  const int nx = c->nx;
+  const double dx = c->lx / (double)nx, g = c->gamma;
+  double *re = malloc(sizeof(double) * nx), *pe = malloc(sizeof(double) * nx);
+  double *fh = calloc((size_t)3 * (nx + 1), 8);
+  orc_fv1d_eq_cells(c, re, pe);
+  for (int f = 1; f < nx; ++f) {
+    double aL[3], aR[3], bL[3], bR[3], p1, p2, p3, p4, w[3], fa[3], fb[3];
+    wb1_face_states(c, d, re, pe, f - 1, dx, aL, aR, &p1, &p2, w);  /* cell left of f */
+    wb1_face_states(c, d, re, pe, f, dx, bL, bR, &p3, &p4, w);      /* cell right of f */
+    fv_flux(g, aR, fa);
+    fv_flux(g, bL, fb);
+    const double cmax = fmax(fv_speed(g, aR), fv_speed(g, bL));
+    for (int v = 0; v < 3; ++v) fh[3 * f + v] = 0.5 * (fb[v] + fa[v]) - 0.5 * cmax * (bL[v] - aR[v]);
+  }
+  for (int i = 1; i < nx - 1; ++i) {
+    double uL[3], uR[3], pL, pR, w[3];
+    wb1_face_states(c, d, re, pe, i, dx, uL, uR, &pL, &pR, w);
+    const double xm = ((double)(i - 1) + 0.5) * dx, xp = ((double)(i + 1) + 0.5) * dx;
+    const double s[3] = {0.0, (pR - pL) / dx, -w[0] * w[1] * c->g * (xp - xm) / (2 * dx)};
+    for (int v = 0; v < 3; ++v)
+      dudt[3 * i + v] = -(fh[3 * (i + 1) + v] - fh[3 * i + v]) / dx + s[v];
+  }
+  for (int v = 0; v < 3; ++v) {
+    dudt[v] = dudt[3 + v];
+    dudt[3 * (nx - 1) + v] = dudt[3 * (nx - 2) + v];
+  }
+  free(re);
+  free(pe);
+  free(fh);
+}
+
 void orc_fv1d_rhs(const orc_fv1d_cfg *c, const double *d, double *dudt) {
+  if (c->scheme == 1) {
+    wb1_rhs(c, d, dudt);
+    return;
+  }
   const int nx = c->nx;
   const double dx = c->lx / (double)nx, g = c->gamma, igm1 = 1.0 / (c->gamma - 1.0);
   double *sl = calloc((size_t)3 * (nx + 2), 8); /* slopes incl. ghosts at 0 and nx+1 */

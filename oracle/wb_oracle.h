@@ -144,6 +144,8 @@ typedef struct {
   int bc;            /* 0 periodic, 1 equilibrium-extrapolated (copy delta) */
   int limiter;       /* 0 first order, 1 minmod MUSCL on delta */
   int eq_kind;       /* ORC_EQ_ISOTHERMAL / ORC_EQ_POLYTROPE */
+  int scheme;        /* 0 'EQL' (equilibrium + delta faces), 1 'WB1' (hydrostatic reconstruction) */
+  int pad0;
   double gamma, g, rho0, p0, kpoly, lx, cfl;
 } orc_fv1d_cfg;
 void orc_fv1d_rhs(const orc_fv1d_cfg *c, const double *delta, double *dudt);

@@ -33,3 +33,30 @@ def test_fv1d_equilibrium_exact(wb):
         n, t = s.evolve(0.25)
         assert n > 10 and abs(t - 0.25) < 1e-15
         assert np.all(s.download() == 0.0)
+
+
+@pytest.mark.parametrize("eq,bc", [(1, 1), (2, 1), (1, 0)])
+def test_wb1_run_parity(wb, orc, eq, bc):
+    """'WB1' (compute_update_sr, benchmark_1d.f90:553-747): the reference's configuration
+    nx = 128, pressure pulse on the atmosphere, t_end = 0.2, CFL 0.8/3."""
+    cfl = 0.8 / 3.0
+    c = orc.make_fv1d(nx=128, bc=bc, limiter=0, eq_kind=eq, cfl=cfl, scheme=1)
+    d0 = orc.fv1d_ic(c)
+    ref, tref, nref = orc.fv1d_run(c, d0, 0.2)
+    with wb.Solver1D(nx=128, bc=bc, limiter=0, eq_kind=eq, cfl=cfl, scheme=wb.SCHEME_WB1) as s:
+        np.testing.assert_allclose(s.compute_update(d0), orc.fv1d_rhs(c, d0), rtol=0, atol=1e-11)
+        s.upload(d0)
+        n, t = s.evolve(0.2)
+        got = s.download()
+    assert n == nref and abs(t - tref) <= 1e-14
+    for v in range(3):
+        assert np.sum(np.abs(got[:, v] - ref[:, v])) <= 1e-9 * (np.sum(np.abs(ref[:, v])) + 1e-30)
+
+
+def test_wb1_polytrope_balanced(wb):
+    with wb.Solver1D(nx=128, limiter=0, eq_kind=2, cfl=0.8 / 3.0, scheme=wb.SCHEME_WB1) as s:
+        z = np.zeros((128, 3))
+        assert np.max(np.abs(s.compute_update(z))) < 1e-12
+        s.upload(z)
+        n, t = s.evolve(0.2)
+        assert n > 10 and np.max(np.abs(s.download())) < 1e-11

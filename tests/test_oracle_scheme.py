@@ -180,3 +180,78 @@ def test_numerical_flux_consistent(orc, riemann):
         exp = np.array([mov[1 + d], mov[1] * v, mov[2] * v, v * (mov[3] + p)])
         exp[1 + d] += p
         np.testing.assert_allclose(f, exp, rtol=1e-14, atol=1e-15)
+
+
+def _wb1_numpy(c, d, orc):
+    """compute_update_sr (benchmark_1d.f90:553-747) written out independently with numpy,
+    on u = u_eq(x_i) + delta_i."""
+    g, nx = c.gamma, c.nx
+    dx = c.lx / nx
+    re, pe = orc.fv1d_eq_cells(c)
+    u = np.stack([re + d[:, 0], d[:, 1], pe / (g - 1) + d[:, 2]])
+    rho, v = u[0], u[1] / u[0]
+    p = (g - 1) * (u[2] - 0.5 * rho * v * v)
+    fl = float(np.float32(1e-5))
+    h = np.maximum(p, fl) / np.maximum(fl, rho) * (1 + 1.0 / (g - 1))
+    x = (np.arange(nx) + 0.5) * dx
+    xf = np.arange(nx + 1) * dx
+    h0l = h + c.g * x - c.g * xf[:-1]
+    h0r = h + c.g * x - c.g * xf[1:]
+    K = np.maximum(fl, p) / np.maximum(fl, rho) ** g
+
+    def state(h0):
+        r = ((1.0 / K) * (g - 1) / g * h0) ** (1 / (g - 1))
+        pp = (1.0 / K) ** (1 / (g - 1)) * ((g - 1) / g * h0) ** (g / (g - 1))
+        return np.stack([r, r * v, pp / (g - 1) + 0.5 * r * v * v]), pp
+
+    uL, pL = state(h0l)
+    uR, pR = state(h0r)
+
+    def flux(uu):
+        vv = uu[1] / uu[0]
+        pp = (g - 1) * (uu[2] - 0.5 * uu[0] * vv * vv)
+        return np.stack([vv * uu[0], vv * uu[1] + pp, vv * uu[2] + pp * vv]), np.abs(vv) + np.sqrt(
+            g * np.maximum(pp, 1e-10) / np.maximum(uu[0], 1e-10))
+
+    fa, sa = flux(uR[:, :-1])   # left cell's right face state, faces 1..nx-1
+    fb, sb = flux(uL[:, 1:])    # right cell's left face state
+    cm = np.maximum(sa, sb)
+    fh = 0.5 * (fb + fa) - 0.5 * cm * (uL[:, 1:] - uR[:, :-1])
+    out = np.zeros((nx, 3))
+    for i in range(1, nx - 1):
+        s = np.array([0.0, (pR[i] - pL[i]) / dx, -rho[i] * v[i] * c.g * (x[i + 1] - x[i - 1]) / (2 * dx)])
+        out[i] = -(fh[:, i] - fh[:, i - 1]) / dx + s
+    out[0], out[-1] = out[1], out[-2]
+    return out
+
+
+@pytest.mark.parametrize("eq_kind", [1, 2])
+def test_wb1_matches_independent_restatement(orc, eq_kind):
+    c = orc.make_fv1d(nx=64, bc=1, limiter=0, eq_kind=eq_kind, scheme=1, cfl=0.8 / 3)
+    rng = np.random.default_rng(eq_kind)
+    d = 1e-3 * rng.standard_normal((64, 3))
+    got = orc.fv1d_rhs(c, d)
+    np.testing.assert_allclose(got, _wb1_numpy(c, d, orc), rtol=0, atol=1e-12)
+
+
+def test_wb1_polytrope_equilibrium_balanced(orc):
+    """'WB1' keeps the isentropic (polytropic) atmosphere to round-off; it is not exact for
+    the isothermal one (K varies from cell to cell), as in the reference."""
+    cp = orc.make_fv1d(nx=128, bc=1, limiter=0, eq_kind=2, scheme=1, cfl=0.8 / 3)
+    z = np.zeros((128, 3))
+    assert np.max(np.abs(orc.fv1d_rhs(cp, z))) < 1e-12
+    d, t, n = orc.fv1d_run(cp, z, 0.2)
+    assert n > 10 and np.max(np.abs(d)) < 1e-11
+    ci = orc.make_fv1d(nx=128, bc=1, limiter=0, eq_kind=1, scheme=1, cfl=0.8 / 3)
+    r = np.max(np.abs(orc.fv1d_rhs(ci, z)))
+    assert 0.0 < r < 1e-2
+
+
+def test_wb1_pressure_pulse(orc):
+    """The reference's WB1 configuration (nx = 128, pressure bump on the isothermal
+    atmosphere, zero-gradient ends, t_end = 0.2, CFL 0.8/3): stays finite, the pulse splits."""
+    c = orc.make_fv1d(nx=128, bc=1, limiter=0, eq_kind=1, scheme=1, cfl=0.8 / 3)
+    d0 = orc.fv1d_ic(c, amp=1e-3)
+    d, t, n = orc.fv1d_run(c, d0, 0.2)
+    assert abs(t - 0.2) < 1e-15 and np.all(np.isfinite(d))
+    assert np.max(np.abs(d[:, 2])) < np.max(np.abs(d0[:, 2]))
