@@ -309,6 +309,10 @@ def run_ours(args):
         host_out = torch.empty(dof, dtype=torch.float32, pin_memory=True)
         s32.download_f32_ptr(host_out.data_ptr())
         host_in.copy_(host_out)
+        # one untimed round trip: first-use costs of the pinned buffers stay out of the timing
+        s32.upload_f32_ptr(host_in.data_ptr())
+        s32.step(1)
+        s32.download_f32_ptr(host_out.data_ptr())
         nE = args.e2e_steps
         barrier(dist)
         t0 = time.perf_counter()

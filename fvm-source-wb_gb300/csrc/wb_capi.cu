@@ -345,9 +345,14 @@ int check_dev_err(wb_ctx *ctx) {
   return WB_OK;
 }
 
-// Limited copy of the resident state in kernel precision, in a free state buffer.
+// Limited copy of the resident state in kernel precision, in a free state buffer (read
+// only for the caller).  Without a limiter the resident state itself is the limited view.
 template <typename R>
 int limited_copy(wb_ctx *ctx, R **out) {
+  if (!(ctx->cfg.limiter && ctx->cfg.order >= 1)) {
+    *out = (R *)state_buf(ctx, 0);
+    return WB_OK;
+  }
   R *dst = (R *)state_buf(ctx, 1);
   CK(cudaMemcpyAsync(dst, state_buf(ctx, 0), ctx->state_bytes, cudaMemcpyDeviceToDevice, ctx->stream));
   if (ctx->cfg.limiter && ctx->cfg.order >= 1) {
