@@ -14,6 +14,10 @@ sys.path.insert(0, os.path.join(ROOT, "tests"))
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (runs through the C ABI)")
+    # the library's tile cache (written by wb_autotune) lives in a per-session file, so
+    # tests never pick up shapes that an earlier run tuned
+    import tempfile
+    os.environ["WB_TILE_CACHE"] = os.path.join(tempfile.mkdtemp(prefix="wbtiles"), "tile_cache.txt")
 
 
 def load_package():
