@@ -118,8 +118,6 @@ StageArgs<R> base_args(const wb_ctx *c) {
   A.hgam = (R)(g.gamma / (g.gamma - 1.0));
   A.gx = (R)g.gx;
   A.gy = (R)g.gy;
-  A.gx4 = (R)(0.25 * g.gx);
-  A.gy4 = (R)(0.25 * g.gy);
   A.rho0 = (R)g.rho0;
   A.p0 = (R)g.p0;
   A.kpoly = (R)g.kpoly;

@@ -119,7 +119,8 @@ __device__ __forceinline__ void flux_lit(const double *u, const double *w, doubl
   }
 }
 
-// Volume point: split fluxes (unscaled) and source (scaled by the 0.25 of the assembly).
+// Volume point: split fluxes (unscaled) and, in FP64, the source (scaled by the 0.25 of
+// the assembly).
 template <typename R>
 __device__ __forceinline__ void vol_point(const StageArgs<R> &A, const R *d, R re, R pe, R *Fx,
                                           R *Fy, R *S) {
@@ -153,8 +154,7 @@ __device__ __forceinline__ void vol_point(const StageArgs<R> &A, const R *d, R r
   } else {
     // exact differences about a static equilibrium (u_eq velocity 0):
     //   d(rho u) = m_x, d(rho u^2 + p) = m_x^2/rho + dp, d(rho u v) = m_x m_y / rho,
-    //   d(u (E+p)) = u (H_eq + dE + dp), dp = (gamma-1)(dE - |m|^2/(2 rho)),
-    //   dS = (0, -drho gx, -drho gy, -(m_x gx + m_y gy))
+    //   d(u (E+p)) = u (H_eq + dE + dp), dp = (gamma-1)(dE - |m|^2/(2 rho))
     R r = rfmax(re + d[0], R(1.0e-9f));
     R inv = frcp(r);
     R vx = d[1] * inv, vy = d[2] * inv;
@@ -168,10 +168,7 @@ __device__ __forceinline__ void vol_point(const StageArgs<R> &A, const R *d, R r
     Fy[1] = d[1] * vy;
     Fy[2] = d[2] * vy + dp;
     Fy[3] = vy * H;
-    S[0] = R(0);
-    S[1] = -(d[0] * A.gx4);
-    S[2] = -(d[0] * A.gy4);
-    S[3] = -(d[1] * A.gx4 + d[2] * A.gy4);
+    (void)S;  // the FP32 form takes the (linear) source from the modes, see tile_compute
   }
 }
 
@@ -578,6 +575,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
                                              double *red, const int tid, const double dt) {
   constexpr int NQ = K + 1;
   constexpr int NB = num_modes(K, BASIS);
+  constexpr bool FP64 = std::is_same<R, double>::value;
   constexpr bool POS = (VAR & WB_VAR_POSITIVITY) != 0;  // positivity limiter compiled in
   constexpr bool HLLC = (VAR & WB_VAR_HLLC) != 0;       // HLLC face flux (else LLF)
   using T = TC<R, K>;
@@ -795,7 +793,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
 #pragma unroll
           for (int v = 0; v < NV; ++v) {
             if (BASIS == 0 || b < K) Pq[v][b] += Fx[v] * T::BW(b, qb);
-            Qq[v][b] += S[v] * T::BW(b, qb);
+            if constexpr (FP64) Qq[v][b] += S[v] * T::BW(b, qb);
             if (b > 0) Qq[v][b] += Fy[v] * dwy;
           }
         }
@@ -810,10 +808,21 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
           constexpr int dummy = 0;
           (void)dummy;
           int a = mode_deg(K, BASIS, m, 0), b = mode_deg(K, BASIS, m, 1);
-          R t = T::BW(a, qa) * Qq[v][b];
-          if (a > 0) t += dwx[a] * Pq[v][b];
-          acc[v][m] += t;
+          if (FP64 || b > 0) acc[v][m] += T::BW(a, qa) * Qq[v][b];
+          if (a > 0) acc[v][m] += dwx[a] * Pq[v][b];
         }
+    }
+    if constexpr (!FP64) {
+      // FP32 form: the gravity source (0, -gx drho, -gy drho, -(gx m_x + gy m_y)) is linear
+      // in the perturbation, so its Gauss projection is exactly -g times the modes
+#pragma unroll
+      for (int m = 0; m < NB; ++m) {
+        const R r = uc[(0 * NB + m) * RXY], mx = uc[(1 * NB + m) * RXY];
+        const R my = uc[(2 * NB + m) * RXY];
+        acc[1][m] -= A.gx * r;
+        acc[2][m] -= A.gy * r;
+        acc[3][m] -= A.gx * mx + A.gy * my;
+      }
     }
     // edge integrals: the faces' moments (already weighted by 0.5/dx, 0.5/dy)
     const int fl = ty * (TX + 1) + tx, fb = ty * TX + tx;

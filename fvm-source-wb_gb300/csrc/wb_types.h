@@ -89,7 +89,6 @@ struct StageArgs {
   R dx, dy, hidx, hidy;       // hidx = 0.5/dx, hidy = 0.5/dy
   R gamma, gm1, igm1, hgam;   // hgam = gamma/(gamma-1)
   R gx, gy;
-  R gx4, gy4;                 // 0.25 gx, 0.25 gy (source weight of the assembly)
   R rho0, p0, kpoly, npoly;   // npoly = 1/(gamma-1)
   R lim_norm, lim_Mdx2, lim_Mdy2, lim_tol;
   R pos_eps;                  // positivity limiter floor (limiter 2)
