@@ -2,11 +2,15 @@
 // well-balanced step: context lifetime, state transfer, the stage loop of evolve, and
 // diagnostics.  Kernels live in the per-precision translation units.
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 #include <dlfcn.h>
 
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <deque>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -37,6 +41,14 @@ struct wb_ctx {
   bool profile = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev;  // recorded stage launches
   std::vector<cudaEvent_t> ev_pool;
+  // TMA descriptors of the state buffers, per staged tile shape (built on first use)
+  struct Tmap {
+    const void *base;
+    int tx, ty;
+    bool ok;
+    CUtensorMap map;
+  };
+  std::deque<Tmap> tmaps;  // stable addresses
 };
 
 namespace {
@@ -200,6 +212,59 @@ int upload_table(wb_ctx *ctx, void **dst, const std::vector<double> &v) {
 
 void *state_buf(wb_ctx *c, int off) { return c->buf[(c->cur + off) % c->nbuf]; }
 
+// cuTensorMapEncodeTiled, from the driver through the runtime (no link to libcuda).
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static std::once_flag once;
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    else
+      cudaGetLastError();
+  });
+  return fn;
+}
+
+// The tensor map that stages a (TX+8) x (TY+2) x planes block of state buffer `base`
+// ([plane][ny][nx], plane stride `plane` elements) into the tile layout of wb_types.h;
+// null where TMA cannot address it (rows not a multiple of 16 bytes) or it is disabled
+// (environment WB_NO_TMA=1).
+const CUtensorMap *state_tmap(wb_ctx *ctx, const void *base, int TX, int TY) {
+  static const bool off = [] {
+    const char *e = std::getenv("WB_NO_TMA");
+    return e && *e && *e != '0';
+  }();
+  if (off) return nullptr;
+  for (auto &m : ctx->tmaps)
+    if (m.base == base && m.tx == TX && m.ty == TY) return m.ok ? &m.map : nullptr;
+  wb_ctx::Tmap m;
+  std::memset(&m, 0, sizeof(m));
+  m.base = base;
+  m.tx = TX;
+  m.ty = TY;
+  const size_t es = ctx->esize;
+  const int planes = NV * ctx->nb;
+  auto encode = tensor_map_encoder();
+  if (encode && ((size_t)ctx->cfg.nx * es) % 16 == 0 && ((size_t)ctx->plane * es) % 16 == 0 &&
+      TX + 8 <= 256 && TY + 2 <= 256 && planes <= 256) {
+    cuuint64_t dims[3] = {(cuuint64_t)ctx->cfg.nx, (cuuint64_t)ctx->cfg.ny, (cuuint64_t)planes};
+    cuuint64_t strides[2] = {(cuuint64_t)ctx->cfg.nx * es, (cuuint64_t)ctx->plane * es};
+    cuuint32_t box[3] = {(cuuint32_t)(TX + 8), (cuuint32_t)(TY + 2), (cuuint32_t)planes};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = encode(&m.map, es == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64,
+                        3, const_cast<void *>(base), dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                        CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    m.ok = r == CUDA_SUCCESS;
+  }
+  ctx->tmaps.push_back(m);
+  return ctx->tmaps.back().ok ? &ctx->tmaps.back().map : nullptr;
+}
+
 // Run one stage of the integrator.
 cudaEvent_t pooled_event(wb_ctx *ctx) {
   if (!ctx->ev_pool.empty()) {
@@ -220,7 +285,16 @@ int launch_stage_R(wb_ctx *ctx, const StageArgs<R> &A) {
     e1 = pooled_event(ctx);
     CK(cudaEventRecord(e0, ctx->stream));
   }
-  CK(launch_stage(A, ctx->cfg.order, ctx->cfg.basis, ctx->TX, ctx->TY, ctx->stream));
+  // interior tiles of a state buffer are staged by TMA (tensor map for the tile the
+  // launch runs)
+  int tx = ctx->TX, ty = ctx->TY;
+  stage_tile(A, ctx->cfg.order, &tx, &ty);
+  const CUtensorMap *tm = nullptr;
+  for (int b = 0; b < ctx->nbuf; ++b)
+    if (A.x == (const R *)ctx->buf[b]) tm = state_tmap(ctx, A.x, tx, ty);
+  StageArgs<R> B = A;
+  B.use_tma = tm != nullptr;
+  CK(launch_stage(B, ctx->cfg.order, ctx->cfg.basis, ctx->TX, ctx->TY, tm, ctx->stream));
   if (ctx->profile) {
     CK(cudaEventRecord(e1, ctx->stream));
     ctx->ev.emplace_back(e0, e1);
@@ -339,6 +413,7 @@ int check_dev_err(wb_ctx *ctx) {
   int e = 0;
   CK(cudaMemcpyAsync(&e, &ctx->dev->err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  if (e & 2) return set_err(ctx, WB_ERR_TIMEOUT, "a bounded device wait (tile copy) gave up");
   if (e) return set_err(ctx, WB_ERR_NONPHYSICAL, "non-finite or non-positive density/pressure in a cell mean");
   return WB_OK;
 }

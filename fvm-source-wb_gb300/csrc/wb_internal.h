@@ -1,6 +1,7 @@
 // wb_internal.h -- entry points between the host layer (wb_capi.cu) and the
 // per-precision kernel translation units.
 #pragma once
+#include <cuda.h>
 #include "wb_types.h"
 
 namespace wb {
@@ -24,10 +25,14 @@ WB_DECLARE_PRECISION_ENTRY_POINTS(double)
 
 // Stage kernels (wb_stage_dispatch.cu): the compiled kernel for precision, degree K,
 // basis and tile TX x TY (and the positivity limiter when the launch needs it).
+// tm: the tensor map of the staged input for the effective tile (stage_tile), or null.
 cudaError_t launch_stage(const StageArgs<float> &A, int K, int basis, int TX, int TY,
-                         cudaStream_t s);
+                         const CUtensorMap *tm, cudaStream_t s);
 cudaError_t launch_stage(const StageArgs<double> &A, int K, int basis, int TX, int TY,
-                         cudaStream_t s);
+                         const CUtensorMap *tm, cudaStream_t s);
+// The tile the launch will run (variants run on the default tile of the precision).
+void stage_tile(const StageArgs<float> &A, int K, int *TX, int *TY);
+void stage_tile(const StageArgs<double> &A, int K, int *TX, int *TY);
 // Tile shapes the stage kernels are compiled for.
 bool tile_supported(int precision_fp32, int tx, int ty);
 

@@ -25,6 +25,7 @@
 // The stage kernels read only the compile-time tables of wb_ctab.h; one translation unit
 // per compiled instance includes this header (wb_stage_instances.h).
 #pragma once
+#include <cuda.h>
 #include <type_traits>
 #include "wb_ctab.h"
 #include "wb_types.h"
@@ -473,6 +474,57 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
 
+// ---------------------------------------------------------------- TMA tile copies
+// One bulk tensor copy stages the modes of an interior tile (tile + one-cell halo, the
+// 16-byte aligned x range [i0-4, i0+TX+4)) into the buffer layout [plane][RY][PX]; its
+// completion is counted on an mbarrier (expect_tx bytes).  Waits are bounded.
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait for phase `parity` of `bar`: false after the iteration limit.
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity) {
+  for (int it = 0; it < (1 << 22); ++it)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+__device__ __forceinline__ void tma_load_3d(void *dst, const void *tmap, int x, int y, int z,
+                                            unsigned long long *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, "
+      "%3, %4}], [%5];\n" ::"r"(smem_u32(dst)),
+      "l"(tmap), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+// Interior tiles whose staged block lies inside the grid: x range [i0-4, i0+TX+4) (a
+// 16-byte aligned start, as TMA requires), rows [j0-1, j0+TY] (no boundary mapping).
+template <int TX, int TY>
+__device__ __forceinline__ bool tma_tile(const int use_tma, const int nx, const int ny,
+                                         const int i0, const int j0) {
+  return use_tma && i0 >= 4 && i0 + TX + 4 <= nx && j0 >= 1 && j0 + TY + 1 <= ny;
+}
+
 // Issue the asynchronous copies that stage one tile (lower-left cell (i0, j0)) into `buf`:
 // the modes of the tile and a one-cell halo, the means of a two-cell halo when the
 // limiter is on, and the tile's equilibrium factors.  Boundary conditions are applied by
@@ -480,7 +532,7 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 template <typename R, int K, int BASIS, int TX, int TY>
 __device__ __forceinline__ void tile_load_async(const StageArgs<R> &A, const bool lim,
                                                 const int i0, const int j0, R *buf,
-                                                const int tid) {
+                                                const int tid, const bool modes = true) {
   constexpr int nthr = TX * TY;
   const TileLayout L = tile_layout(K, BASIS, TX, TY, lim);
   const int lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
@@ -493,7 +545,9 @@ __device__ __forceinline__ void tile_load_async(const StageArgs<R> &A, const boo
   // 16-byte chunks (rows still BC-mapped in y); otherwise element-wise with x mapping
   const bool vec = i0 >= 4 && i0 + TX + 4 <= nx && (nx % VEC) == 0;
   const int nrow = NV * L.NB * L.RY;
-  if (vec) {
+  if (!modes) {
+    // the modes come by TMA (k_stage)
+  } else if (vec) {
     for (int k = tid; k < nrow * CPR; k += nthr) {
       const int row = k / CPR, ch = k - row * CPR;
       const int pl = row / L.RY, ry = row - pl * L.RY;
@@ -943,15 +997,19 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
 // HLLC face flux; the default kernel carries neither.
 template <typename R, int K, int BASIS, int TX, int TY, int VAR>
 __global__ void __launch_bounds__(TX *TY, std::is_same<R, float>::value ? 2 : 1)
-    k_stage(const __grid_constant__ StageArgs<R> A) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+    k_stage(const __grid_constant__ StageArgs<R> A, const __grid_constant__ CUtensorMap tmap) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   const int tid = threadIdx.x;
   const bool lim = A.limiter == 1 && A.lim_y && K >= 1;  // minmod: stage the means halo
   const TileLayout L = tile_layout(K, BASIS, TX, TY, lim);
   double *red = reinterpret_cast<double *>(smem_raw);
+  // two mbarriers (one per staging buffer) after the reduction scratch
+  unsigned long long *bar = reinterpret_cast<unsigned long long *>(smem_raw) + 48;
   R *bufs = reinterpret_cast<R *>(smem_raw + 64 * sizeof(double));
   R *flux = bufs + 2 * L.buf;
-  const int ntx = (A.nx + TX - 1) / TX, nty = (A.ny + TY - 1) / TY, ntiles = ntx * nty;
+  const int nx = A.nx, ny = A.ny;
+  const int ntx = (nx + TX - 1) / TX, nty = (ny + TY - 1) / TY, ntiles = ntx * nty;
+  const unsigned tma_bytes = (unsigned)(NV * L.NB * L.RY * L.PX * sizeof(R));
   const double dt = stage_dt(A);
   if (A.advance_time && blockIdx.x == 0 && tid == 0) {
     DevState *S = A.dev;
@@ -960,24 +1018,58 @@ __global__ void __launch_bounds__(TX *TY, std::is_same<R, float>::value ? 2 : 1)
     S->smax[A.parity ^ 1][0] = 0ull;
     S->smax[A.parity ^ 1][1] = 0ull;
   }
-  int t = blockIdx.x;
-  if (t < ntiles) tile_load_async<R, K, BASIS, TX, TY>(A, lim, (t % ntx) * TX, (t / ntx) * TY, bufs, tid);
-  cp_async_commit();
-  if (t + (int)gridDim.x < ntiles) {
-    const int t1 = t + gridDim.x;
-    tile_load_async<R, K, BASIS, TX, TY>(A, lim, (t1 % ntx) * TX, (t1 / ntx) * TY, bufs + L.buf, tid);
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_fence_init();
   }
+  __syncthreads();
+  // stage tile `tl` into buffer b: one TMA copy for an interior tile's modes (thread 0
+  // arms the buffer's mbarrier), cp.async for the rest
+  // TMA destinations must be 128-byte aligned: checked, never assumed
+  const int use_tma = A.use_tma && (smem_u32(bufs) & 127u) == 0u &&
+                      ((L.buf * (int)sizeof(R)) & 127) == 0;
+  bool pending[2] = {false, false};  // a TMA copy into buffer b not yet waited for
+  unsigned phase[2] = {0u, 0u};
+  auto stage = [&](const int tl, const int b) {
+    const int i0 = (tl % ntx) * TX, j0 = (tl / ntx) * TY;
+    R *buf = bufs + b * L.buf;
+    const bool tma = tma_tile<TX, TY>(use_tma, nx, ny, i0, j0);
+    if (tma && tid == 0) {
+      mbar_expect_tx(&bar[b], tma_bytes);
+      tma_load_3d(buf + L.su, &tmap, i0 - 4, j0 - 1, 0, &bar[b]);
+    }
+    pending[b] = tma;
+    tile_load_async<R, K, BASIS, TX, TY>(A, lim, i0, j0, buf, tid, !tma);
+  };
+  bool ok = true;
+  int t = blockIdx.x;
+  if (t < ntiles) stage(t, 0);
+  cp_async_commit();
+  if (t + (int)gridDim.x < ntiles) stage(t + gridDim.x, 1);
   cp_async_commit();
   for (int k = 0; t < ntiles; t += gridDim.x, ++k) {
+    const int b = k & 1;
     cp_async_wait<1>();
-    __syncthreads();
-    R *buf = bufs + (k & 1) * L.buf;
+    if (pending[b]) {
+      if (mbar_wait(&bar[b], phase[b])) {
+        phase[b] ^= 1u;
+        pending[b] = false;
+      } else {  // stays pending: the exit path waits for it once more
+        atomicOr(&A.dev->err, 2);
+        ok = false;
+      }
+    }
+    if (__syncthreads_or(!ok)) break;
+    R *buf = bufs + b * L.buf;
     tile_compute<R, K, BASIS, TX, TY, VAR>(A, lim, (t % ntx) * TX, (t / ntx) * TY, buf, flux, red, tid, dt);
     const int tn = t + 2 * (int)gridDim.x;
-    if (tn < ntiles)
-      tile_load_async<R, K, BASIS, TX, TY>(A, lim, (tn % ntx) * TX, (tn / ntx) * TY, buf, tid);
+    if (tn < ntiles) stage(tn, b);
     cp_async_commit();
   }
+  // nothing may still be copying into shared memory when the CTA exits
+  for (int b = 0; b < 2; ++b)
+    if (pending[b]) (void)mbar_wait(&bar[b], phase[b]);
   cp_async_wait<0>();
 }
 

@@ -1,16 +1,20 @@
 // wb_stage_launch.cuh -- launch of one persistent stage kernel.  Included by the
 // per-instance translation units that build.py generates from wb_stage_instances.h.
 #pragma once
+#include <cstring>
 #include "wb_stage.cuh"
 #include "wb_stage_instances.h"
 
 namespace wb {
 
 template <typename R, int K, int BASIS, int TX, int TY, int VAR>
-static cudaError_t launch_stage_kernel(const StageArgs<R> &A, cudaStream_t s) {
+static cudaError_t launch_stage_kernel(const StageArgs<R> &A, const CUtensorMap *tm,
+                                       cudaStream_t s) {
   const int lim = A.limiter == 1 && A.lim_y && K >= 1;
   const size_t smem = stage_smem_bytes<R>(K, BASIS, TX, TY, lim);
   auto kern = k_stage<R, K, BASIS, TX, TY, VAR>;
+  CUtensorMap none;
+  std::memset(&none, 0, sizeof(none));
   static int per_sm[2] = {0, 0};  // occupancy per limiter setting, queried once
   if (per_sm[lim] == 0) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -32,7 +36,7 @@ static cudaError_t launch_stage_kernel(const StageArgs<R> &A, cudaStream_t s) {
   const long long ntiles = (long long)((A.nx + TX - 1) / TX) * ((A.ny + TY - 1) / TY);
   long long grid = (long long)nsm * per_sm[lim];
   if (grid > ntiles) grid = ntiles;
-  kern<<<(unsigned)grid, TX * TY, smem, s>>>(A);
+  kern<<<(unsigned)grid, TX * TY, smem, s>>>(A, tm ? *tm : none);
   return cudaGetLastError();
 }
 
@@ -41,8 +45,8 @@ static cudaError_t launch_stage_kernel(const StageArgs<R> &A, cudaStream_t s) {
 // One compiled stage kernel (a line of wb_stage_instances.h) and its launcher.
 #define WB_STAGE_INSTANCE(P, R, K, BT, B, TX, TY, VAR)                                      \
   namespace wb {                                                                            \
-  cudaError_t WB_STAGE_INSTANCE_NAME(P, K, BT, TX, TY, VAR)(const StageArgs<R> &A,          \
-                                                            cudaStream_t s) {               \
-    return launch_stage_kernel<R, K, B, TX, TY, VAR>(A, s);                                 \
+  cudaError_t WB_STAGE_INSTANCE_NAME(P, K, BT, TX, TY, VAR)(                                 \
+      const StageArgs<R> &A, const CUtensorMap *tm, cudaStream_t s) {                       \
+    return launch_stage_kernel<R, K, B, TX, TY, VAR>(A, tm, s);                             \
   }                                                                                         \
   }

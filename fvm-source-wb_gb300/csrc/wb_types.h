@@ -59,7 +59,7 @@ struct DevState {
   double t[2];
   unsigned long long smax[2][2];  // [parity][direction]
   long long nstep[2];
-  int err;
+  int err;  // bit 0: non-physical cell mean; bit 1: a bounded device wait gave up
   int pad;
 };
 
@@ -85,6 +85,7 @@ struct StageArgs {
   long long plane;            // elements between (var, mode) planes
   int bc_x, bc_y, llf_speed, limiter, lim_y;  // limiter: 0 off, 1 minmod, 2 positivity
   int riemann;                // 0 LLF, 1 HLLC (the kernel variant must match)
+  int use_tma;                // interior tiles staged by one TMA copy (tensor map given)
   int eq_kind;
   R dx, dy, hidx, hidy;       // hidx = 0.5/dx, hidy = 0.5/dy
   R gamma, gm1, igm1, hgam;   // hgam = gamma/(gamma-1)
@@ -135,7 +136,7 @@ __host__ __device__ inline TileLayout tile_layout(int K, int basis, int TX, int 
   L.sm = NV * L.NB * L.RXY;
   L.eq = L.sm + (lim ? NV * L.LY * L.PX : 0);
   const int neq = L.NQ * (TX + 2) + TX + 1 + L.NQ * (TY + 2) + TY + 1;
-  L.buf = (L.eq + neq + 3) & ~3;  // 16-byte aligned double buffers
+  L.buf = (L.eq + neq + 31) & ~31;  // 128-byte aligned double buffers (TMA destinations)
   return L;
 }
 // Largest tile width the staging code handles (three 32-wide chunks of a halo row).
