@@ -682,8 +682,12 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
 
   // 3. faces, x and y in one balanced loop: x face (fi, fj) sits between tile cells
   //    fi-1 and fi of row fj; y face (fi, fj) between rows fj-1 and fj of column fi
-  for (int fa = tid; fa < FXS + FYS; fa += nthr) {
-    if (fa < FXS) {
+  // The y faces start at a warp boundary (x range padded to a multiple of 32), so no
+  // warp runs both face kinds in one pass: a warp's passes are all x or all y.
+  const int FXP = (FXS + 31) & ~31;
+  for (int fa = tid; fa < FXP + FYS; fa += nthr) {
+    if (fa < FXP) {
+    if (fa >= FXS) continue;
     const int f = fa;
     int fi = f % (TX + 1), fj = f / (TX + 1);
     int gfi = i0 + fi, gj = j0 + fj;
@@ -737,7 +741,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
 #pragma unroll
       for (int b = 0; b < NQ; ++b) sfx[(v * NQ + b) * FXS + f] = mom[v][b] * A.hidx;
     } else {
-    const int f = fa - FXS;
+    const int f = fa - FXP;
     int fi = f % TX, fj = f / TX;
     int gi = i0 + fi, gfj = j0 + fj;
     if (gi >= nx || gfj > ny) continue;
