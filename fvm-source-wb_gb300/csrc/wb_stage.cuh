@@ -627,7 +627,8 @@ template <typename R, int K, int BASIS, int TX, int TY, int VAR>
 __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool lim_,
                                              const int i0, const int j0, R *buf, R *flux,
                                              double *red, const int tid, const double dt,
-                                             double *speed_acc = nullptr) {
+                                             double *speed_acc = nullptr,
+                                             const bool end_sync = true) {
   constexpr int NQ = K + 1;
   constexpr int NB = num_modes(K, BASIS);
   constexpr bool FP64 = std::is_same<R, double>::value;
@@ -999,7 +1000,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
       }
     }
   }
-  __syncthreads();
+  if (end_sync) __syncthreads();
 }
 
 // Persistent stage kernel: CTAs stride over the tiles of the grid; the next-but-one
@@ -1056,14 +1057,16 @@ __global__ void __launch_bounds__(TX *TY, std::is_same<R, float>::value ? 2 : 1)
   };
   bool ok = true;
   double speed[2] = {0.0, 0.0};  // this thread's wave-speed maxima over its tiles
+  // Pipeline: tile t is staged while tile t - G is computed.  The barrier after tile t's
+  // data arrives also frees tile t - G's buffer and the flux area, so the next tile's
+  // copies are issued right after it and tile_compute needs no closing barrier.
+  const int G = gridDim.x;
   int t = blockIdx.x;
   if (t < ntiles) stage(t, 0);
   cp_async_commit();
-  if (t + (int)gridDim.x < ntiles) stage(t + gridDim.x, 1);
-  cp_async_commit();
-  for (int k = 0; t < ntiles; t += gridDim.x, ++k) {
+  for (int k = 0; t < ntiles; t += G, ++k) {
     const int b = k & 1;
-    cp_async_wait<1>();
+    cp_async_wait<0>();
     if (pending[b]) {
       if (mbar_wait(&bar[b], phase[b])) {
         phase[b] ^= 1u;
@@ -1074,13 +1077,13 @@ __global__ void __launch_bounds__(TX *TY, std::is_same<R, float>::value ? 2 : 1)
       }
     }
     if (__syncthreads_or(!ok)) break;
+    if (t + G < ntiles) stage(t + G, b ^ 1);
+    cp_async_commit();
     R *buf = bufs + b * L.buf;
     tile_compute<R, K, BASIS, TX, TY, VAR>(A, lim, (t % ntx) * TX, (t / ntx) * TY, buf, flux, red,
-                                           tid, dt, speed);
-    const int tn = t + 2 * (int)gridDim.x;
-    if (tn < ntiles) stage(tn, b);
-    cp_async_commit();
+                                           tid, dt, speed, false);
   }
+  __syncthreads();  // the last tile's readers are done before the reduction reuses `red`
   // wave-speed maxima of all this CTA's tiles: one block reduction per launch
   if (A.compute_speed) {
     const double mx = block_max(speed[0], red, tid, TX * TY);
