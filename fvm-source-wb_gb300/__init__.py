@@ -77,6 +77,7 @@ def lib():
             "wb_num_modes": ([i32, i32], i32), "wb_mode_list": ([i32, i32, p, p], i32),
             "wb_upload_state": ([p, p, i32], i32), "wb_download_state": ([p, p, i32], i32),
             "wb_upload_state_f32": ([p, p], i32), "wb_download_state_f32": ([p, p], i32),
+            "wb_step_io_f32": ([p, p, p, i32, ctypes.c_double], i32),
             "wb_download_state_raw": ([p, p], i32),
             "wb_init_perturbation": ([p, p], i32), "wb_device_state": ([p, p, p], i32),
             "wb_compute_update": ([p, p, p, i32], i32), "wb_apply_limiter": ([p], i32),
@@ -443,6 +444,12 @@ class Solver:
     def upload_f32_ptr(self, host_ptr):
         """Upload from a raw host address holding a dense float32 SoA state."""
         self._check(lib().wb_upload_state_f32(self._ctx, ctypes.c_void_p(host_ptr)))
+
+    def step_io_f32_ptr(self, in_ptr, out_ptr, nsteps=1, dt=-1.0):
+        """Pipelined: upload from in_ptr, step, download into out_ptr; returns at once.
+        Both host buffers belong to the library until sync()."""
+        self._check(lib().wb_step_io_f32(self._ctx, ctypes.c_void_p(in_ptr),
+                                         ctypes.c_void_p(out_ptr), int(nsteps), float(dt)))
 
     def download_f32_ptr(self, host_ptr):
         self._check(lib().wb_download_state_f32(self._ctx, ctypes.c_void_p(host_ptr)))

@@ -49,6 +49,12 @@ struct wb_ctx {
     CUtensorMap map;
   };
   std::deque<Tmap> tmaps;  // stable addresses
+  // pipelined host I/O (wb_step_io_f32): copy streams, ping-pong device staging, events
+  bool io_init = false;
+  int io_k = 0;
+  cudaStream_t s_in = nullptr, s_out = nullptr;
+  void *io_in[2] = {nullptr, nullptr}, *io_out[2] = {nullptr, nullptr};
+  cudaEvent_t in_ready[2] = {}, in_free[2] = {}, out_ready[2] = {}, out_free[2] = {};
 };
 
 namespace {
@@ -633,6 +639,20 @@ int wb_destroy(wb_ctx *ctx) {
     cudaEventDestroy(p.second);
   }
   for (auto e : ctx->ev_pool) cudaEventDestroy(e);
+  if (ctx->io_init) {
+    cudaStreamSynchronize(ctx->s_in);
+    cudaStreamSynchronize(ctx->s_out);
+    for (int k = 0; k < 2; ++k) {
+      cudaFree(ctx->io_in[k]);
+      cudaFree(ctx->io_out[k]);
+      cudaEventDestroy(ctx->in_ready[k]);
+      cudaEventDestroy(ctx->in_free[k]);
+      cudaEventDestroy(ctx->out_ready[k]);
+      cudaEventDestroy(ctx->out_free[k]);
+    }
+    cudaStreamDestroy(ctx->s_in);
+    cudaStreamDestroy(ctx->s_out);
+  }
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return WB_OK;
@@ -984,7 +1004,62 @@ int wb_autotune(wb_ctx *ctx, int32_t steps, int32_t *tile_x, int32_t *tile_y) {
 int wb_sync(wb_ctx *ctx) {
   if (!ctx) return WB_ERR_ARG;
   CK(cudaSetDevice(ctx->cfg.device));
+  if (ctx->io_init) {
+    CK(cudaStreamSynchronize(ctx->s_in));
+    CK(cudaStreamSynchronize(ctx->s_out));
+  }
   return check_dev_err(ctx);
+}
+
+int wb_step_io_f32(wb_ctx *ctx, const float *in, float *out, int32_t nsteps, double dt) {
+  if (!ctx || !in || !out || nsteps < 0) return WB_ERR_ARG;
+  if (!is_fp32(ctx)) return set_err(ctx, WB_ERR_STATE, "wb_step_io_f32 needs an FP32 context");
+  CK(cudaSetDevice(ctx->cfg.device));
+  if (!ctx->io_init) {
+    CK(cudaStreamCreateWithFlags(&ctx->s_in, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&ctx->s_out, cudaStreamNonBlocking));
+    for (int k = 0; k < 2; ++k) {
+      int rc;
+      if ((rc = dalloc(ctx, (char **)&ctx->io_in[k], ctx->state_bytes))) return rc;
+      if ((rc = dalloc(ctx, (char **)&ctx->io_out[k], ctx->state_bytes))) return rc;
+      CK(cudaEventCreateWithFlags(&ctx->in_ready[k], cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&ctx->in_free[k], cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&ctx->out_ready[k], cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&ctx->out_free[k], cudaEventDisableTiming));
+    }
+    ctx->io_init = true;
+  }
+  const int k = ctx->io_k & 1;
+  ++ctx->io_k;
+  const size_t rowb = (size_t)ctx->ncell * sizeof(float), pitch = ctx->plane * sizeof(float);
+  const int nrow = NV * ctx->nb;
+  // 1. input: host -> staging buffer k (free once the compute stream took its last input)
+  CK(cudaStreamWaitEvent(ctx->s_in, ctx->in_free[k], 0));
+  CK(cudaMemcpy2DAsync(ctx->io_in[k], pitch, in, rowb, rowb, nrow, cudaMemcpyHostToDevice,
+                       ctx->s_in));
+  CK(cudaEventRecord(ctx->in_ready[k], ctx->s_in));
+  // 2. compute stream: take the input as the state, step, leave the limited result
+  CK(cudaStreamWaitEvent(ctx->stream, ctx->in_ready[k], 0));
+  CK(cudaMemcpyAsync(state_buf(ctx, 0), ctx->io_in[k], ctx->state_bytes, cudaMemcpyDeviceToDevice,
+                     ctx->stream));
+  CK(cudaEventRecord(ctx->in_free[k], ctx->stream));
+  ctx->speed_valid = false;
+  int rc = step_impl(ctx, nsteps, dt > 0.0 ? 0 : 1, dt, -1.0);
+  if (rc) return rc;
+  CK(cudaStreamWaitEvent(ctx->stream, ctx->out_free[k], 0));
+  CK(cudaMemcpyAsync(ctx->io_out[k], state_buf(ctx, 0), ctx->state_bytes,
+                     cudaMemcpyDeviceToDevice, ctx->stream));
+  if (ctx->cfg.limiter && ctx->cfg.order >= 1) {
+    StageArgs<float> A = base_args<float>(ctx);
+    CK(launch_limit(A, (float *)ctx->io_out[k], ctx->cfg.order, ctx->cfg.basis, ctx->stream));
+  }
+  CK(cudaEventRecord(ctx->out_ready[k], ctx->stream));
+  // 3. output: staging buffer k -> host
+  CK(cudaStreamWaitEvent(ctx->s_out, ctx->out_ready[k], 0));
+  CK(cudaMemcpy2DAsync(out, rowb, ctx->io_out[k], pitch, rowb, nrow, cudaMemcpyDeviceToHost,
+                       ctx->s_out));
+  CK(cudaEventRecord(ctx->out_free[k], ctx->s_out));
+  return WB_OK;
 }
 
 int wb_get_time(wb_ctx *ctx, double *t, int64_t *steps) {

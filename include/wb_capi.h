@@ -119,6 +119,14 @@ int wb_download_state(wb_ctx *ctx, double *delta, int32_t layout);
 /* same with FP32 host arrays (SoA only) */
 int wb_upload_state_f32(wb_ctx *ctx, const float *delta);
 int wb_download_state_f32(wb_ctx *ctx, float *delta);
+/* Pipelined host I/O (FP32 contexts): enqueues the upload of `in` as the state, `nsteps`
+ * steps (dt > 0 fixed, else CFL) and the download of the limited result into `out`, and
+ * returns at once.  Successive calls overlap: the upload of call k+1 and the download of
+ * call k-1 run on their own streams while call k steps (ping-pong device staging).
+ * `in` and `out` (dense SoA float arrays, page-locked for the copies to be asynchronous)
+ * belong to the library until wb_sync.  Time and step counter continue across calls.
+ * (No reference routine: the host-to-device pipeline of a drop-in driver.) */
+int wb_step_io_f32(wb_ctx *ctx, const float *in, float *out, int32_t nsteps, double dt);
 /* The resident state exactly as stored (SoA; double for FP64 contexts, float for FP32),
  * before the limit-on-load: what a checkpoint needs so that a restart through
  * wb_upload_state / wb_upload_state_f32 continues bit for bit.  (No reference routine:
@@ -154,7 +162,7 @@ int wb_step(wb_ctx *ctx, int32_t nsteps, double dt);
  * 2d/benchmark_2d_dg.f90:624-775.  Synchronising. */
 int wb_evolve(wb_ctx *ctx, double tend, int32_t max_steps, int32_t *steps_done, double *t_out);
 /* Waits for the context stream; reports a device-side non-physical flag. */
-int wb_sync(wb_ctx *ctx);
+int wb_sync(wb_ctx *ctx);  /* also completes wb_step_io_f32 copies */
 int wb_get_time(wb_ctx *ctx, double *t, int64_t *steps);
 /* Sets the simulated time and step counter (checkpoint restart; the reference keeps t
  * in evolve's locals and has no restart). */

@@ -83,3 +83,27 @@ def test_autotune_preserves_state(wb, tmp_path, monkeypatch):
     with solver(wb, c, 1) as s2:   # a new context picks the cached shape up
         s2.upload(d)
         assert s2.autotune(1) in [(32, 8), (16, 16)]
+
+
+def test_step_io_pipeline_matches_sync_calls(wb):
+    """wb_step_io_f32 (pipelined upload / steps / download) gives, call for call, what
+    upload + step + download give."""
+    import torch
+    c = base_cfg(nx=40, ny=24, order=2, basis=1, eq_kind=1, limiter=1, bc_x=0)
+    n = 3
+    ins = [random_delta(c, amp=1e-2, seed=20 + k).astype(np.float32) for k in range(n)]
+    with solver(wb, c, 1) as a, solver(wb, c, 1) as b:
+        dof = a.dofs
+        hin = [torch.from_numpy(x.reshape(-1).copy()).pin_memory() for x in ins]
+        hout = [torch.empty(dof, dtype=torch.float32, pin_memory=True) for _ in range(n)]
+        for k in range(n):
+            a.step_io_f32_ptr(hin[k].data_ptr(), hout[k].data_ptr(), 2, 1e-3)
+        a.sync()
+        for k in range(n):
+            b.upload_f32(ins[k])
+            b.step(2, 1e-3)
+            ref = b.download_f32()
+            np.testing.assert_array_equal(hout[k].numpy().reshape(ref.shape), ref)
+        ta, na = a.time()
+        tb, nb = b.time()
+        assert na == nb == 2 * n and ta == tb
