@@ -78,6 +78,7 @@ def lib():
             "wb_upload_state": ([p, p, i32], i32), "wb_download_state": ([p, p, i32], i32),
             "wb_upload_state_f32": ([p, p], i32), "wb_download_state_f32": ([p, p], i32),
             "wb_step_io_f32": ([p, p, p, i32, ctypes.c_double], i32),
+            "wb_selftest_wait_timeout": ([p, i32], i32),
             "wb_download_state_raw": ([p, p], i32),
             "wb_init_perturbation": ([p, p], i32), "wb_device_state": ([p, p, p], i32),
             "wb_compute_update": ([p, p, p, i32], i32), "wb_apply_limiter": ([p], i32),
@@ -444,6 +445,10 @@ class Solver:
     def upload_f32_ptr(self, host_ptr):
         """Upload from a raw host address holding a dense float32 SoA state."""
         self._check(lib().wb_upload_state_f32(self._ctx, ctypes.c_void_p(host_ptr)))
+
+    def selftest_wait_timeout(self, polls=4096):
+        """Status of the bounded-wait self-test (WB_ERR_TIMEOUT expected)."""
+        return lib().wb_selftest_wait_timeout(self._ctx, int(polls))
 
     def step_io_f32_ptr(self, in_ptr, out_ptr, nsteps=1, dt=-1.0):
         """Pipelined: upload from in_ptr, step, download into out_ptr; returns at once.

@@ -1011,6 +1011,18 @@ int wb_sync(wb_ctx *ctx) {
   return check_dev_err(ctx);
 }
 
+int wb_selftest_wait_timeout(wb_ctx *ctx, int32_t polls) {
+  if (!ctx || polls < 1) return WB_ERR_ARG;
+  CK(cudaSetDevice(ctx->cfg.device));
+  int e = 0;
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(launch_wait_selftest(&ctx->dev->err, polls, ctx->stream));
+  CK(cudaMemcpyAsync(&e, &ctx->dev->err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemsetAsync(&ctx->dev->err, 0, sizeof(int), ctx->stream));  // context stays usable
+  CK(cudaStreamSynchronize(ctx->stream));
+  return (e & 2) ? WB_ERR_TIMEOUT : WB_OK;
+}
+
 int wb_step_io_f32(wb_ctx *ctx, const float *in, float *out, int32_t nsteps, double dt) {
   if (!ctx || !in || !out || nsteps < 0) return WB_ERR_ARG;
   if (!is_fp32(ctx)) return set_err(ctx, WB_ERR_STATE, "wb_step_io_f32 needs an FP32 context");

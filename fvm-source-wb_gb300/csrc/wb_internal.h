@@ -48,6 +48,7 @@ cudaError_t launch_norms(const AuxArgs &A, const Tab1D<double> *Td, const double
                          const double *b, double *partial, double *out, int K, int basis,
                          cudaStream_t s);
 cudaError_t launch_f32_to_f64(double *out, const float *in, long long n, cudaStream_t s);
+cudaError_t launch_wait_selftest(int *err, int polls, cudaStream_t s);
 cudaError_t launch_f64_to_f32(float *out, const double *in, long long n, cudaStream_t s);
 
 // batched form (FP32): persistent stage over a work list; per-instance max speed

@@ -22,6 +22,25 @@ cudaError_t launch_norms(const AuxArgs &A, const Tab1D<double> *Td, const double
   return cudaGetLastError();
 }
 
+// Self-test of the bounded device wait of the TMA staging: an mbarrier whose phase nothing
+// completes.  The wait gives up after `polls` polls and reports it in the error word, as a
+// stage kernel would; nothing is in flight when the kernel returns.
+__global__ void k_wait_selftest(int *err, int polls) {
+  __shared__ unsigned long long bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  const bool done = mbar_wait(&bar, 0u, polls);
+  if (!done && threadIdx.x == 0) atomicOr(err, 2);
+}
+
+cudaError_t launch_wait_selftest(int *err, int polls, cudaStream_t s) {
+  k_wait_selftest<<<1, 32, 0, s>>>(err, polls);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_f32_to_f64(double *out, const float *in, long long n, cudaStream_t s) {
   k_convert<double, float><<<1216, 256, 0, s>>>(out, in, n);
   return cudaGetLastError();

@@ -503,9 +503,10 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned 
       : "memory");
   return ok != 0;
 }
-// Bounded wait for phase `parity` of `bar`: false after the iteration limit.
-__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity) {
-  for (int it = 0; it < (1 << 22); ++it)
+// Bounded wait for phase `parity` of `bar`: false after `limit` polls.
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity,
+                                          int limit = 1 << 22) {
+  for (int it = 0; it < limit; ++it)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }

@@ -127,6 +127,12 @@ int wb_download_state_f32(wb_ctx *ctx, float *delta);
  * belong to the library until wb_sync.  Time and step counter continue across calls.
  * (No reference routine: the host-to-device pipeline of a drop-in driver.) */
 int wb_step_io_f32(wb_ctx *ctx, const float *in, float *out, int32_t nsteps, double dt);
+/* Failure-detection self-test: runs the bounded device wait of the tile staging (the
+ * mbarrier wait of the TMA copies) on a barrier that nothing completes, limited to
+ * `polls` polls.  Returns WB_ERR_TIMEOUT (the expected result: the wait gave up and
+ * reported it through the context's error word), then clears the word so the context
+ * stays usable. */
+int wb_selftest_wait_timeout(wb_ctx *ctx, int32_t polls);
 /* The resident state exactly as stored (SoA; double for FP64 contexts, float for FP32),
  * before the limit-on-load: what a checkpoint needs so that a restart through
  * wb_upload_state / wb_upload_state_f32 continues bit for bit.  (No reference routine:

@@ -107,3 +107,20 @@ def test_step_io_pipeline_matches_sync_calls(wb):
         ta, na = a.time()
         tb, nb = b.time()
         assert na == nb == 2 * n and ta == tb
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_bounded_wait_reports_timeout_and_context_survives(wb, precision):
+    """Failure detection without a fault: the staging's mbarrier wait on a barrier that
+    nothing completes gives up after its poll limit, the host reads WB_ERR_TIMEOUT, and
+    the context keeps working."""
+    c = base_cfg(nx=48, ny=40, order=2, basis=1, eq_kind=1)
+    d = random_delta(c, amp=1e-2, seed=3)
+    with solver(wb, c, precision) as s, solver(wb, c, precision) as ref:
+        assert s.selftest_wait_timeout(4096) == wb.WB_ERR_TIMEOUT
+        s.upload(d)
+        ref.upload(d)
+        s.step(3)
+        ref.step(3)
+        s.sync()
+        np.testing.assert_array_equal(s.download(), ref.download())
