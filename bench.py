@@ -366,6 +366,47 @@ def run_ours(args):
     return 0
 
 
+def run_accuracy(args):
+    """The accuracy configuration (cfg3): 2048^2 P2 polytrope K = 1, Phi = y, seeded Gaussian
+    pressure bump (sigma 0.05) of amplitude 1e-1, 1e-3 and 1e-6; the FP32 perturbation form
+    against the FP64 plain method over the same fixed time steps (dt from the initial CFL
+    speed of the FP64 run).  Prints one JSON line: L1 / Linf per conserved variable of the
+    difference (unit-area domain, so L1 is a mean absolute error) and of the perturbation."""
+    import torch
+    wb = load_package()
+    wb.lib()
+    torch.cuda.set_device(0)
+    n = args.accuracy_steps
+    results = []
+    for amp in (1e-1, 1e-3, 1e-6):
+        w64 = wb.workload("cfg3", wb.PREC_FP64)
+        w32 = wb.workload("cfg3", wb.PREC_FP32)
+        ic = wb.workload_ic("cfg3", amp)
+        with wb.Solver(**w64) as s64, wb.Solver(**w32) as s32:
+            s64.init_perturbation(ic)
+            s32.init_perturbation(ic)
+            sx, sy = s64.compute_max_speed()
+            dx, dy = w64["lx"] / w64["nx"], w64["ly"] / w64["ny"]
+            dt = w64["cfl"] / (2 * w64["order"] + 1) / (sx / dx + sy / dy)
+            t0 = time.perf_counter()
+            s64.step(n, dt)
+            s32.step(n, dt)
+            s64.sync()
+            s32.sync()
+            el = time.perf_counter() - t0
+            l1, linf, _ = s32.compute_error(s64)
+            p1, pinf, _ = s64.compute_error(None)
+        results.append({"amplitude": amp, "l1_fp32_vs_fp64": l1.tolist(),
+                        "linf_fp32_vs_fp64": linf.tolist(), "l1_perturbation": p1.tolist(),
+                        "linf_perturbation": pinf.tolist(), "dt": dt, "seconds": el,
+                        "pass": bool(np.all(l1 <= 1e-6))})
+    print(json.dumps({"mode": "accuracy",
+                      "workload": "cfg3: 2048^2 P2 polytrope K=1, Phi=y, Gaussian pressure bump "
+                                  "(sigma 0.05, seed 3), FP32 perturbation vs FP64 plain",
+                      "steps": n, "l1_bar": 1e-6, "results": results}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -383,11 +424,16 @@ def main():
                     help="cells per side instead of the workload's (small cases for profiling)")
     ap.add_argument("--tile", default="", help="fixed stage tile TXxTY (default: autotune)")
     ap.add_argument("--quick", action="store_true", help="skip FP64, accuracy and CPU legs")
+    ap.add_argument("--accuracy", action="store_true",
+                    help="run the cfg3 accuracy study instead of the benchmark")
+    ap.add_argument("--accuracy-steps", type=int, default=500)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.accuracy:
+        return run_accuracy(args)
     return run_ours(args)
 
 
