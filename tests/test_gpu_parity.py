@@ -273,3 +273,21 @@ def test_steps_parity_interior_tiles(wb, orc, nx, ny, limiter, precision):
         got = s.download()
     bar = 1e-12 if precision == 0 else 1e-6
     assert np.all(rel_l1_full(c, got, ref) < bar)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("riemann,integrator", [(1, 0), (0, 1), (1, 1)])
+def test_variants_on_interior_tiles(wb, orc, precision, riemann, integrator):
+    """HLLC and SSP-RK(5,4) on a grid with TMA-staged tiles (the variant kernels run the
+    default tile of the precision)."""
+    c = base_cfg(nx=128, ny=72, order=2, basis=1, eq_kind=2, gx=0.0, gy=1.0, bc_x=0, bc_y=1,
+                 riemann=riemann, limiter=1)
+    d = random_delta(c, amp=1e-2, seed=17)
+    run = orc.run_rk2 if integrator == 0 else orc.run_rk54
+    ref, _ = run(orc_cfg(c), d, 4, 1e-3)
+    with solver(wb, c, precision, integrator) as s:
+        s.upload(d)
+        s.step(4, 1e-3)
+        got = s.download()
+    bar = 1e-12 if precision == 0 else 1e-6
+    assert np.all(rel_l1_full(c, got, ref) < bar)
