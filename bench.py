@@ -272,6 +272,7 @@ def run_ours(args):
         w64 = wb.workload(name, wb.PREC_FP64, **size)
         s64 = wb.Solver(device=dev, **w64)
         s64.init_perturbation(ic)
+        tile64 = s64.autotune(1)
         s64.step(1)
         s64.sync()
         st64 = torch.cuda.ExternalStream(s64.stream(), device=dev)
@@ -297,6 +298,7 @@ def run_ours(args):
         s32b.close()
         s64.close()
         extra["fp64_plain"] = {"value": v64, "unit": UNIT, "steps": args.plain_steps,
+                               "tile": list(tile64),
                                "speedup_fp32_over_fp64": value / world / v64}
         extra["accuracy"] = {"l1_fp32_vs_fp64": l1.tolist(), "linf_fp32_vs_fp64": linf.tolist(),
                              "l1_perturbation_fp64": ref1.tolist(), "steps": args.check_steps,

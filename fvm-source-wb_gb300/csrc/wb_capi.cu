@@ -104,7 +104,7 @@ int validate(const wb_config *c, std::string &why) {
   if (c->tile_x > 0 || c->tile_y > 0) {
     long long t = (long long)c->tile_x * c->tile_y;
     if (!tile_supported(c->precision == WB_PREC_FP32, c->tile_x, c->tile_y))
-      return why = "tile shape not compiled (FP32: 32x8, 16x16; FP64: 16x8)", WB_ERR_CONFIG;
+      return why = "tile shape not compiled (FP32: 32x8, 16x16; FP64: 16x8, 16x4)", WB_ERR_CONFIG;
     (void)t;
   }
   return WB_OK;
@@ -946,8 +946,8 @@ int wb_autotune(wb_ctx *ctx, int32_t steps, int32_t *tile_x, int32_t *tile_y) {
   CK(cudaSetDevice(ctx->cfg.device));
   const int fp32 = is_fp32(ctx);
   const int cand[2][2] = {{32, 8}, {16, 16}};
-  const int ncand = fp32 ? 2 : 1;
-  const int c64[1][2] = {{16, 8}};
+  const int ncand = 2;
+  const int c64[2][2] = {{16, 8}, {16, 4}};
   // save the run so every candidate starts from the same state
   void *backup = nullptr;
   int rc = dalloc(ctx, (char **)&backup, ctx->state_bytes);

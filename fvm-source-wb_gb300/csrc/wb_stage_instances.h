@@ -33,20 +33,25 @@
   X(f32, float, 2, p, 1, 32, 8, 2) \
   X(f32, float, 2, p, 1, 32, 8, 3) \
   X(f64, double, 0, p, 1, 16, 8, 0) \
+  X(f64, double, 0, p, 1, 16, 4, 0) \
   X(f64, double, 0, p, 1, 16, 8, 2) \
   X(f64, double, 1, q, 0, 16, 8, 0) \
+  X(f64, double, 1, q, 0, 16, 4, 0) \
   X(f64, double, 1, q, 0, 16, 8, 1) \
   X(f64, double, 1, q, 0, 16, 8, 2) \
   X(f64, double, 1, q, 0, 16, 8, 3) \
   X(f64, double, 1, p, 1, 16, 8, 0) \
+  X(f64, double, 1, p, 1, 16, 4, 0) \
   X(f64, double, 1, p, 1, 16, 8, 1) \
   X(f64, double, 1, p, 1, 16, 8, 2) \
   X(f64, double, 1, p, 1, 16, 8, 3) \
   X(f64, double, 2, q, 0, 16, 8, 0) \
+  X(f64, double, 2, q, 0, 16, 4, 0) \
   X(f64, double, 2, q, 0, 16, 8, 1) \
   X(f64, double, 2, q, 0, 16, 8, 2) \
   X(f64, double, 2, q, 0, 16, 8, 3) \
   X(f64, double, 2, p, 1, 16, 8, 0) \
+  X(f64, double, 2, p, 1, 16, 4, 0) \
   X(f64, double, 2, p, 1, 16, 8, 1) \
   X(f64, double, 2, p, 1, 16, 8, 2) \
   X(f64, double, 2, p, 1, 16, 8, 3)

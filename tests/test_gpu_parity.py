@@ -226,7 +226,7 @@ def test_tiles_agree(wb, precision):
     c = base_cfg(nx=37, ny=23, order=2, basis=1, limiter=1)
     d = random_delta(c, seed=21)
     outs = []
-    tiles = [(32, 8), (16, 16)] if precision == 1 else [(16, 8)]
+    tiles = [(32, 8), (16, 16)] if precision == 1 else [(16, 8), (16, 4)]
     for tx, ty in tiles:
         with solver(wb, c, precision, tile_x=tx, tile_y=ty) as s:
             s.upload(d)
@@ -273,6 +273,22 @@ def test_steps_parity_interior_tiles(wb, orc, nx, ny, limiter, precision):
         got = s.download()
     bar = 1e-12 if precision == 0 else 1e-6
     assert np.all(rel_l1_full(c, got, ref) < bar)
+
+
+def test_fp64_tiles_agree_on_interior_tiles(wb, orc):
+    """The two FP64 tiles (16x8, 16x4) on a grid with TMA-staged tiles, against the oracle."""
+    c = base_cfg(nx=128, ny=72, order=2, basis=1, eq_kind=1, gx=0.0, gy=1.0, bc_x=0, bc_y=1,
+                 limiter=1)
+    d = random_delta(c, amp=1e-2, seed=9)
+    ref, _ = orc.run_rk2(orc_cfg(c), d, 4, 1e-3)
+    outs = []
+    for tx, ty in [(16, 8), (16, 4)]:
+        with solver(wb, c, 0, tile_x=tx, tile_y=ty) as s:
+            s.upload(d)
+            s.step(4, 1e-3)
+            outs.append(s.download())
+    np.testing.assert_array_equal(outs[0], outs[1])
+    assert np.all(rel_l1_full(c, outs[1], ref) < 1e-12)
 
 
 @pytest.mark.parametrize("precision", [0, 1])
