@@ -34,8 +34,8 @@ __device__ __forceinline__ void item_load(const StageArgs<R> *__restrict__ args,
   else tile_load_async<R, 2, 1, BATCH_TX, BATCH_TY>(A, lim, w.y, w.z, buf, tid);
 }
 
-// Persistent batched stage: CTAs stride over the work list; the next-but-one item is
-// staged (cp.async) while the current one is computed.  bufsz = the largest tile buffer.
+// Persistent batched stage: CTAs stride over the work list; the next item is staged
+// (cp.async) while the current one is computed.  bufsz = the largest tile buffer.
 template <typename R, bool POS>
 __global__ void __launch_bounds__(256, 2)
     k_batch_stage(const StageArgs<R> *__restrict__ args, const int4 *__restrict__ items, int nitems,
@@ -46,14 +46,18 @@ __global__ void __launch_bounds__(256, 2)
   double *red = reinterpret_cast<double *>(smem_raw);
   R *bufs = reinterpret_cast<R *>(smem_raw + 64 * sizeof(double));
   R *flux = bufs + 2 * bufsz;
+  // Item it is staged while item it - G is computed; the barrier after its arrival also
+  // frees the previous item's buffer, argument slot and flux area (as in k_stage).
+  const int G = gridDim.x;
   int it = blockIdx.x;
   if (it < nitems) item_load(args, items[it], sA[0], bufs, tid, nthr);
   cp_async_commit();
-  if (it + (int)gridDim.x < nitems) item_load(args, items[it + gridDim.x], sA[1], bufs + bufsz, tid, nthr);
-  cp_async_commit();
-  for (int k = 0; it < nitems; it += gridDim.x, ++k) {
-    cp_async_wait<1>();
+  for (int k = 0; it < nitems; it += G, ++k) {
+    cp_async_wait<0>();
     __syncthreads();
+    if (it + G < nitems)
+      item_load(args, items[it + G], sA[(k + 1) & 1], bufs + ((k + 1) & 1) * bufsz, tid, nthr);
+    cp_async_commit();
     const int4 w = items[it];
     int K, TX, TY;
     unpack_item(w, K, TX, TY);
@@ -68,12 +72,9 @@ __global__ void __launch_bounds__(256, 2)
       S->smax[A.parity ^ 1][1] = 0ull;
     }
     const bool lim = A.limiter == 1 && A.lim_y && K >= 1;
-    if (K == 0) tile_compute<R, 0, 1, BATCH_TX, BATCH_TY, POS ? WB_VAR_POSITIVITY : 0>(A, lim, w.y, w.z, buf, flux, red, tid, dt);
-    else if (K == 1) tile_compute<R, 1, 1, BATCH_TX, BATCH_TY, POS ? WB_VAR_POSITIVITY : 0>(A, lim, w.y, w.z, buf, flux, red, tid, dt);
-    else tile_compute<R, 2, 1, BATCH_TX, BATCH_TY, POS ? WB_VAR_POSITIVITY : 0>(A, lim, w.y, w.z, buf, flux, red, tid, dt);
-    const int in = it + 2 * (int)gridDim.x;
-    if (in < nitems) item_load(args, items[in], sA[k & 1], buf, tid, nthr);
-    cp_async_commit();
+    if (K == 0) tile_compute<R, 0, 1, BATCH_TX, BATCH_TY, POS ? WB_VAR_POSITIVITY : 0>(A, lim, w.y, w.z, buf, flux, red, tid, dt, nullptr, false);
+    else if (K == 1) tile_compute<R, 1, 1, BATCH_TX, BATCH_TY, POS ? WB_VAR_POSITIVITY : 0>(A, lim, w.y, w.z, buf, flux, red, tid, dt, nullptr, false);
+    else tile_compute<R, 2, 1, BATCH_TX, BATCH_TY, POS ? WB_VAR_POSITIVITY : 0>(A, lim, w.y, w.z, buf, flux, red, tid, dt, nullptr, false);
   }
   cp_async_wait<0>();
 }
