@@ -79,6 +79,7 @@ def lib():
             "wb_upload_state_f32": ([p, p], i32), "wb_download_state_f32": ([p, p], i32),
             "wb_step_io_f32": ([p, p, p, i32, ctypes.c_double], i32),
             "wb_selftest_wait_timeout": ([p, i32], i32),
+            "wb_set_equilibrium": ([p, i32, ctypes.c_double, ctypes.c_double, p], i32),
             "wb_download_state_raw": ([p, p], i32),
             "wb_init_perturbation": ([p, p], i32), "wb_device_state": ([p, p, p], i32),
             "wb_compute_update": ([p, p, p, i32], i32), "wb_apply_limiter": ([p], i32),
@@ -445,6 +446,19 @@ class Solver:
     def upload_f32_ptr(self, host_ptr):
         """Upload from a raw host address holding a dense float32 SoA state."""
         self._check(lib().wb_upload_state_f32(self._ctx, ctypes.c_void_p(host_ptr)))
+
+    def set_equilibrium(self, eq_kind, gx, gy, rho0=None, p0=None, kpoly=None):
+        """Replace the hydrostatic equilibrium; the perturbation state is kept."""
+        params = None
+        if rho0 is not None or p0 is not None or kpoly is not None:
+            params = np.array([self.cfg.rho0 if rho0 is None else rho0,
+                               self.cfg.p0 if p0 is None else p0,
+                               self.cfg.kpoly if kpoly is None else kpoly], dtype=np.float64)
+        self._check(lib().wb_set_equilibrium(self._ctx, int(eq_kind), float(gx), float(gy),
+                                             _ptr(params) if params is not None else None))
+        self.cfg.eq_kind, self.cfg.gx, self.cfg.gy = eq_kind, gx, gy
+        if params is not None:
+            self.cfg.rho0, self.cfg.p0, self.cfg.kpoly = params
 
     def selftest_wait_timeout(self, polls=4096):
         """Status of the bounded-wait self-test (WB_ERR_TIMEOUT expected)."""

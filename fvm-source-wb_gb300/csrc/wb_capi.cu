@@ -210,9 +210,36 @@ int ensure_scratch(wb_ctx *ctx) {
 template <typename R>
 int upload_table(wb_ctx *ctx, void **dst, const std::vector<double> &v) {
   std::vector<R> h(v.begin(), v.end());
-  int rc = dalloc(ctx, (R **)dst, h.size() * sizeof(R));
-  if (rc) return rc;
+  if (*dst == nullptr) {  // first build allocates; a rebuild overwrites in place
+    int rc = dalloc(ctx, (R **)dst, h.size() * sizeof(R));
+    if (rc) return rc;
+  }
   CK(cudaMemcpy(*dst, h.data(), h.size() * sizeof(R), cudaMemcpyHostToDevice));
+  return WB_OK;
+}
+
+// Equilibrium factor tables of ctx->cfg (FP64 copy, and the kernel-precision copy).
+int build_eq_tables(wb_ctx *ctx, const double *xq) {
+  const wb_config *cfg = &ctx->cfg;
+  EqParams ep{cfg->eq_kind, cfg->gamma, cfg->gx, cfg->gy, cfg->rho0, cfg->p0, cfg->kpoly};
+  std::vector<double> fxv, fxf, fyv, fyf;
+  make_eq_tables(ep, cfg->nx, cfg->ny, cfg->lx, cfg->ly, ctx->nq, xq, fxv, fxf, fyv, fyf);
+  int rc;
+  if ((rc = upload_table<double>(ctx, (void **)&ctx->fxv64, fxv))) return rc;
+  if ((rc = upload_table<double>(ctx, (void **)&ctx->fxf64, fxf))) return rc;
+  if ((rc = upload_table<double>(ctx, (void **)&ctx->fyv64, fyv))) return rc;
+  if ((rc = upload_table<double>(ctx, (void **)&ctx->fyf64, fyf))) return rc;
+  if (is_fp32(ctx)) {
+    if ((rc = upload_table<float>(ctx, &ctx->fxv, fxv))) return rc;
+    if ((rc = upload_table<float>(ctx, &ctx->fxf, fxf))) return rc;
+    if ((rc = upload_table<float>(ctx, &ctx->fyv, fyv))) return rc;
+    if ((rc = upload_table<float>(ctx, &ctx->fyf, fyf))) return rc;
+  } else {
+    if ((rc = upload_table<double>(ctx, &ctx->fxv, fxv))) return rc;
+    if ((rc = upload_table<double>(ctx, &ctx->fxf, fxf))) return rc;
+    if ((rc = upload_table<double>(ctx, &ctx->fyv, fyv))) return rc;
+    if ((rc = upload_table<double>(ctx, &ctx->fyf, fyf))) return rc;
+  }
   return WB_OK;
 }
 
@@ -705,24 +732,7 @@ int wb_create(const wb_config *cfg, wb_ctx **out) {
   if ((rc = dalloc(ctx, &ctx->Td, sizeof(t64)))) return rc;
   CK(cudaMemcpy(ctx->Td, t64, sizeof(t64), cudaMemcpyHostToDevice));
   // equilibrium factor tables
-  EqParams ep{cfg->eq_kind, cfg->gamma, cfg->gx, cfg->gy, cfg->rho0, cfg->p0, cfg->kpoly};
-  std::vector<double> fxv, fxf, fyv, fyf;
-  make_eq_tables(ep, cfg->nx, cfg->ny, cfg->lx, cfg->ly, ctx->nq, t64[K].xq, fxv, fxf, fyv, fyf);
-  if ((rc = upload_table<double>(ctx, (void **)&ctx->fxv64, fxv))) return rc;
-  if ((rc = upload_table<double>(ctx, (void **)&ctx->fxf64, fxf))) return rc;
-  if ((rc = upload_table<double>(ctx, (void **)&ctx->fyv64, fyv))) return rc;
-  if ((rc = upload_table<double>(ctx, (void **)&ctx->fyf64, fyf))) return rc;
-  if (is_fp32(ctx)) {
-    if ((rc = upload_table<float>(ctx, &ctx->fxv, fxv))) return rc;
-    if ((rc = upload_table<float>(ctx, &ctx->fxf, fxf))) return rc;
-    if ((rc = upload_table<float>(ctx, &ctx->fyv, fyv))) return rc;
-    if ((rc = upload_table<float>(ctx, &ctx->fyf, fyf))) return rc;
-  } else {
-    if ((rc = upload_table<double>(ctx, &ctx->fxv, fxv))) return rc;
-    if ((rc = upload_table<double>(ctx, &ctx->fxf, fxf))) return rc;
-    if ((rc = upload_table<double>(ctx, &ctx->fyv, fyv))) return rc;
-    if ((rc = upload_table<double>(ctx, &ctx->fyf, fyf))) return rc;
-  }
+  if ((rc = build_eq_tables(ctx, t64[K].xq))) return rc;
   for (int b = 0; b < ctx->nbuf; ++b) {
     if ((rc = dalloc(ctx, (char **)&ctx->buf[b], ctx->state_bytes))) return rc;
     CK(cudaMemsetAsync(ctx->buf[b], 0, ctx->state_bytes, ctx->stream));
@@ -1009,6 +1019,34 @@ int wb_sync(wb_ctx *ctx) {
     CK(cudaStreamSynchronize(ctx->s_out));
   }
   return check_dev_err(ctx);
+}
+
+int wb_set_equilibrium(wb_ctx *ctx, int32_t kind, double gx, double gy, const double *params) {
+  if (!ctx) return WB_ERR_ARG;
+  wb_config c = ctx->cfg;
+  c.eq_kind = kind;
+  c.gx = gx;
+  c.gy = gy;
+  if (params) {
+    c.rho0 = params[0];
+    c.p0 = params[1];
+    c.kpoly = params[2];
+  }
+  std::string why;
+  if (int v = validate(&c, why)) return set_err(ctx, v, why);
+  CK(cudaSetDevice(ctx->cfg.device));
+  CK(cudaStreamSynchronize(ctx->stream));  // in-flight stages read the old tables
+  if (ctx->io_init) {
+    CK(cudaStreamSynchronize(ctx->s_in));
+    CK(cudaStreamSynchronize(ctx->s_out));
+  }
+  ctx->cfg = c;
+  Tab1D<double> t64[KMAX + 1];
+  make_tab1d(t64);
+  int rc = build_eq_tables(ctx, t64[ctx->cfg.order].xq);
+  if (rc) return rc;
+  ctx->speed_valid = false;
+  return WB_OK;
 }
 
 int wb_selftest_wait_timeout(wb_ctx *ctx, int32_t polls) {

@@ -106,6 +106,11 @@ int wb_config_default(wb_config *cfg);
 int wb_create(const wb_config *cfg, wb_ctx **out);
 int wb_destroy(wb_ctx *ctx);
 const char *wb_last_error(const wb_ctx *ctx);
+/* Replaces the context's hydrostatic equilibrium (get_equilibrium_solution,
+ * 2d/benchmark_2d_dg.f90:594-622): kind WB_EQ_*, Phi = gx x + gy y, params = {rho0, p0,
+ * kpoly} (null keeps them).  Validated like wb_create; the perturbation state is kept (it
+ * is now a perturbation of the new equilibrium); waits for the context's work first. */
+int wb_set_equilibrium(wb_ctx *ctx, int32_t kind, double gx, double gy, const double *params);
 const char *wb_status_string(int status);
 /* number of modes per variable; the (a,b) degree list in the library's order */
 int wb_num_modes(int order, int basis);

@@ -124,3 +124,29 @@ def test_bounded_wait_reports_timeout_and_context_survives(wb, precision):
         ref.step(3)
         s.sync()
         np.testing.assert_array_equal(s.download(), ref.download())
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_set_equilibrium_matches_fresh_context(wb, precision):
+    """wb_set_equilibrium swaps the equilibrium tables in place: steps after the switch are
+    bit for bit those of a context created with the new equilibrium, and a zero
+    perturbation of the new equilibrium stays at rest."""
+    c0 = base_cfg(nx=40, ny=24, order=2, basis=1, eq_kind=1, gx=1.0, gy=1.0, limiter=1)
+    c1 = dict(c0, eq_kind=2, gx=0.3, gy=-0.7, rho0=1.2, p0=0.9, kpoly=0.8)
+    d = random_delta(c0, amp=1e-2, seed=31)
+    with solver(wb, c0, precision) as a, solver(wb, c1, precision) as b:
+        a.upload(d)
+        a.step(2, 1e-3)
+        a.set_equilibrium(2, 0.3, -0.7, rho0=1.2, p0=0.9, kpoly=0.8)
+        assert (a.cfg.eq_kind, a.cfg.gx, a.cfg.rho0) == (2, 0.3, 1.2)
+        mid = a.download()
+        b.upload(mid)
+        a.step(3, 1e-3)
+        b.step(3, 1e-3)
+        np.testing.assert_array_equal(a.download(), b.download())
+        a.upload(np.zeros_like(d))
+        a.step(4)
+        assert np.abs(a.download()).max() < (1e-5 if precision else 1e-12)
+        with pytest.raises(RuntimeError):
+            a.set_equilibrium(7, 0.0, 0.0)
+        assert a.cfg.eq_kind == 2   # a rejected call changes nothing
