@@ -20,7 +20,9 @@
 //              (dg_with_source.f90:1749-2031 applied pointwise);
 //   float   -- "perturbation": exact difference algebra for zero equilibrium
 //              velocity, so a zero perturbation gives an exactly zero update and
-//              no O(1) equilibrium quantity is ever subtracted in FP32.
+//              no O(1) equilibrium quantity is ever subtracted in FP32.  Its volume
+//              quadrature and LLF faces run on packed f32x2 pairs (__ffma2_rn and
+//              friends), which halves the issue slots of that arithmetic.
 //
 // The stage kernels read only the compile-time tables of wb_ctab.h; one translation unit
 // per compiled instance includes this header (wb_stage_instances.h).
@@ -293,6 +295,47 @@ __device__ __forceinline__ void face_point(const StageArgs<R> &A, const R *dL, c
 #pragma unroll
       for (int v = 0; v < NV; ++v) F[v] = R(0.5) * (fR[v] + fL[v]) + R(0.5) * lam * (dL[v] - dR[v]);
     }
+  }
+}
+
+// FP32 LLF face point on packed pairs (sm_100+ f32x2 arithmetic: one instruction for two
+// lanes): d2[v] = (left, right) perturbation traces, the two sides' exact-difference
+// fluxes and sound speeds computed side by side.  Returns F[v] = 2 (F_hat - F(u_eq))
+// = (f_L + lam d_L) + (f_R - lam d_R); the caller folds the 0.5 into its edge weights.
+template <int DIR>
+__device__ __forceinline__ void face_point_pk(const StageArgs<float> &A, const float2 *d2,
+                                              float re, float pe, float *F) {
+  float2 r2 = __fadd2_rn(make_float2(re, re), d2[0]);
+  r2.x = rfmax(r2.x, 1.0e-9f);
+  r2.y = rfmax(r2.y, 1.0e-9f);
+  const float2 inv = make_float2(frcp(r2.x), frcp(r2.y));
+  const float2 vx = __fmul2_rn(d2[1], inv), vy = __fmul2_rn(d2[2], inv);
+  const float2 ke = __ffma2_rn(d2[2], vy, __fmul2_rn(d2[1], vx));
+  const float2 dp = __fmul2_rn(make_float2(A.gm1, A.gm1),
+                               __ffma2_rn(make_float2(-0.5f, -0.5f), ke, d2[3]));
+  const float hp = A.hgam * pe;
+  const float2 H = __fadd2_rn(__fadd2_rn(make_float2(hp, hp), d2[3]), dp);
+  const float2 vn = DIR == 0 ? vx : vy;
+  float2 f[NV];
+  f[0] = d2[1 + DIR];
+  f[1] = DIR == 0 ? __ffma2_rn(d2[1], vx, dp) : __fmul2_rn(d2[1], vy);
+  f[2] = DIR == 0 ? __fmul2_rn(d2[2], vx) : __ffma2_rn(d2[2], vy, dp);
+  f[3] = __fmul2_rn(vn, H);
+  float2 pp = __fadd2_rn(make_float2(pe, pe), dp);
+  pp.x = rfmax(pp.x, 1e-10f);
+  pp.y = rfmax(pp.y, 1e-10f);
+  const float2 c2 = __fmul2_rn(__fmul2_rn(make_float2(A.gamma, A.gamma), pp), inv);
+  const float cL = fsqrt_pos(c2.x), cR = fsqrt_pos(c2.y);
+  float lam;
+  if (A.llf_speed == 1)
+    lam = rfmax(fabsf(vn.y + cR), fabsf(vn.x + cL));
+  else
+    lam = rfmax(fabsf(vn.x) + cL, fabsf(vn.y) + cR);
+  const float2 l2 = make_float2(lam, -lam);
+#pragma unroll
+  for (int v = 0; v < NV; ++v) {
+    const float2 g = __ffma2_rn(l2, d2[v], f[v]);
+    F[v] = g.x + g.y;
   }
 }
 
@@ -635,6 +678,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
   constexpr bool FP64 = std::is_same<R, double>::value;
   constexpr bool POS = (VAR & WB_VAR_POSITIVITY) != 0;  // positivity limiter compiled in
   constexpr bool HLLC = (VAR & WB_VAR_HLLC) != 0;       // HLLC face flux (else LLF)
+  constexpr bool PKF = !FP64 && !HLLC;                  // packed FP32 LLF faces
   using T = TC<R, K>;
   const TileLayout L = tile_layout(K, BASIS, TX, TY, lim_);
   // RX / LX below are the stored row pitch (TX + 8); the staged ring starts at column 3
@@ -695,6 +739,51 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
     int gfi = i0 + fi, gj = j0 + fj;
     if (gfi > nx || gj >= ny) continue;
     (void)gj;
+    if constexpr (PKF) {
+      // packed (left, right) pairs through traces, point values and the flux
+      float2 clr[NV][NQ];
+#pragma unroll
+      for (int v = 0; v < NV; ++v)
+#pragma unroll
+        for (int b = 0; b < NQ; ++b) {
+          float2 s2 = make_float2(0.f, 0.f);
+#pragma unroll
+          for (int a = 0; a < NQ; ++a) {
+            int m = mode_index(K, BASIS, a, b);
+            if (m < 0) continue;
+            const R *pm = su + (v * NB + m) * RXY + (fj + 1) * RX;
+            s2 = __ffma2_rn(make_float2(pm[fi], pm[fi + 1]), make_float2(T::Ep(a), T::Em(a)), s2);
+          }
+          clr[v][b] = s2;
+        }
+      const float fxf = sfxf[fi];
+      float mom[NV][NQ];
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) {
+        float2 d2[NV];
+        float F[NV], re, pe;
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          float2 s2 = make_float2(0.f, 0.f);
+#pragma unroll
+          for (int b = 0; b < NQ; ++b)
+            s2 = __ffma2_rn(clr[v][b], make_float2(T::B(b, q), T::B(b, q)), s2);
+          d2[v] = s2;
+        }
+        eq_point(A, fxf, sfyv[fj * NQ + q], re, pe);
+        face_point_pk<0>(A, d2, re, pe, F);
+#pragma unroll
+        for (int v = 0; v < NV; ++v)
+#pragma unroll
+          for (int b = 0; b < NQ; ++b)
+            mom[v][b] = (q == 0 ? 0.f : mom[v][b]) + F[v] * (0.5f * T::BW(b, q));
+      }
+#pragma unroll
+      for (int v = 0; v < NV; ++v)
+#pragma unroll
+        for (int b = 0; b < NQ; ++b) sfx[(v * NQ + b) * FXS + f] = mom[v][b] * A.hidx;
+      continue;
+    }
     R cl[NV][NQ], cr[NV][NQ];
 #pragma unroll
     for (int v = 0; v < NV; ++v)
@@ -747,6 +836,52 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
     int fi = f % TX, fj = f / TX;
     int gi = i0 + fi, gfj = j0 + fj;
     if (gi >= nx || gfj > ny) continue;
+    if constexpr (PKF) {
+      // packed (bottom, top) pairs
+      float2 cbt[NV][NQ];
+#pragma unroll
+      for (int v = 0; v < NV; ++v)
+#pragma unroll
+        for (int a = 0; a < NQ; ++a) {
+          float2 s2 = make_float2(0.f, 0.f);
+#pragma unroll
+          for (int b = 0; b < NQ; ++b) {
+            int m = mode_index(K, BASIS, a, b);
+            if (m < 0) continue;
+            const R *pm = su + (v * NB + m) * RXY + (fi + 1);
+            s2 = __ffma2_rn(make_float2(pm[fj * RX], pm[(fj + 1) * RX]),
+                            make_float2(T::Ep(b), T::Em(b)), s2);
+          }
+          cbt[v][a] = s2;
+        }
+      const float fyf = sfyf[fj];
+      float mom[NV][NQ];
+#pragma unroll
+      for (int q = 0; q < NQ; ++q) {
+        float2 d2[NV];
+        float F[NV], re, pe;
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          float2 s2 = make_float2(0.f, 0.f);
+#pragma unroll
+          for (int a = 0; a < NQ; ++a)
+            s2 = __ffma2_rn(cbt[v][a], make_float2(T::B(a, q), T::B(a, q)), s2);
+          d2[v] = s2;
+        }
+        eq_point(A, sfxv[fi * NQ + q], fyf, re, pe);
+        face_point_pk<1>(A, d2, re, pe, F);
+#pragma unroll
+        for (int v = 0; v < NV; ++v)
+#pragma unroll
+          for (int a = 0; a < NQ; ++a)
+            mom[v][a] = (q == 0 ? 0.f : mom[v][a]) + F[v] * (0.5f * T::BW(a, q));
+      }
+#pragma unroll
+      for (int v = 0; v < NV; ++v)
+#pragma unroll
+        for (int a = 0; a < NQ; ++a) sfy[(v * NQ + a) * FYS + f] = mom[v][a] * A.hidy;
+      continue;
+    }
     R cb[NV][NQ], ct[NV][NQ];
 #pragma unroll
     for (int v = 0; v < NV; ++v)
@@ -808,8 +943,94 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
 #pragma unroll
       for (int m = 0; m < NB; ++m) acc[v][m] = R(0);
     R rbar = R(0), pbar = R(0);
-    // the qa loop stays rolled: a third of the code for the volume quadrature, which
+    // the qa loops stay rolled: a third of the code for the volume quadrature, which
     // measured faster (fewer instruction-fetch stalls) than full unrolling
+    if constexpr (!FP64) {
+      // FP32 on packed pairs: point values as (rho, E) and (m_x, m_y), split fluxes as
+      // (Fx, Fy) of one variable, projections as (P_b, Q_{b+1}) with P_b = sum Fx BW(b),
+      // Q_b = sum Fy DW(b) (the 0.5/dy goes into bwy below)
+#pragma unroll 1
+      for (int qa = 0; qa < NQ; ++qa) {
+        float2 cre[NQ], cmm[NQ];
+#pragma unroll
+        for (int b = 0; b < NQ; ++b) {
+          float2 s1 = make_float2(0.f, 0.f), s2 = make_float2(0.f, 0.f);
+#pragma unroll
+          for (int a = 0; a < NQ; ++a) {
+            int m = mode_index(K, BASIS, a, b);
+            if (m < 0) continue;
+            const float2 B2 = make_float2(T::B(a, qa), T::B(a, qa));
+            s1 = __ffma2_rn(make_float2(uc[(0 * NB + m) * RXY], uc[(3 * NB + m) * RXY]), B2, s1);
+            s2 = __ffma2_rn(make_float2(uc[(1 * NB + m) * RXY], uc[(2 * NB + m) * RXY]), B2, s2);
+          }
+          cre[b] = s1;
+          cmm[b] = s2;
+        }
+        const float fx = sfxv[tx * NQ + qa];
+        float2 PQ[NV][K > 0 ? K : 1];
+        float PK[NV];  // P_K, needed by the tensor basis only
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          PK[v] = 0.f;
+#pragma unroll
+          for (int b = 0; b < K; ++b) PQ[v][b] = make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int qb = 0; qb < NQ; ++qb) {
+          float2 dre = make_float2(0.f, 0.f), dm = make_float2(0.f, 0.f);
+#pragma unroll
+          for (int b = 0; b < NQ; ++b) {
+            const float2 B2 = make_float2(T::B(b, qb), T::B(b, qb));
+            dre = __ffma2_rn(cre[b], B2, dre);
+            dm = __ffma2_rn(cmm[b], B2, dm);
+          }
+          float re, pe;
+          eq_point(A, fx, sfyv[ty * NQ + qb], re, pe);
+          if (A.compute_speed) {
+            float ww = 0.25f * T::wq(qa) * T::wq(qb);
+            rbar += re * ww;
+            pbar += pe * ww;
+          }
+          // vol_point's exact differences, (x, y) side by side
+          const float r = rfmax(re + dre.x, 1.0e-9f);
+          const float inv = frcp(r);
+          const float2 vel = __fmul2_rn(dm, make_float2(inv, inv));
+          const float dp = A.gm1 * (dre.y - 0.5f * (dm.x * vel.x + dm.y * vel.y));
+          const float H = A.hgam * pe + dre.y + dp;
+          float2 F[NV];
+          F[0] = dm;
+          F[1] = __ffma2_rn(make_float2(dm.x, dm.x), vel, make_float2(dp, 0.f));
+          F[2] = __ffma2_rn(make_float2(dm.y, dm.y), vel, make_float2(0.f, dp));
+          F[3] = __fmul2_rn(vel, make_float2(H, H));
+#pragma unroll
+          for (int b = 0; b < K; ++b) {
+            const float2 W2 = make_float2(T::BW(b, qb), T::DW(b + 1, qb));
+#pragma unroll
+            for (int v = 0; v < NV; ++v) PQ[v][b] = __ffma2_rn(F[v], W2, PQ[v][b]);
+          }
+          if constexpr (BASIS == 0) {
+#pragma unroll
+            for (int v = 0; v < NV; ++v) PK[v] += F[v].x * T::BW(K, qb);
+          }
+        }
+        float dwx[NQ], bwy[NQ];
+#pragma unroll
+        for (int a = 0; a < NQ; ++a) {
+          dwx[a] = A.hidx * T::DW(a, qa);
+          bwy[a] = A.hidy * T::BW(a, qa);
+        }
+#pragma unroll
+        for (int v = 0; v < NV; ++v)
+#pragma unroll
+          for (int m = 0; m < NB; ++m) {
+            constexpr int dummy = 0;
+            (void)dummy;
+            int a = mode_deg(K, BASIS, m, 0), b = mode_deg(K, BASIS, m, 1);
+            if (b > 0) acc[v][m] += bwy[a] * PQ[v][b - 1].y;
+            if (a > 0) acc[v][m] += dwx[a] * (b < K ? PQ[v][b].x : PK[v]);
+          }
+      }
+    } else {
 #pragma unroll 1
     for (int qa = 0; qa < NQ; ++qa) {
       R c[NV][NQ];
@@ -874,6 +1095,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
           if (FP64 || b > 0) acc[v][m] += T::BW(a, qa) * Qq[v][b];
           if (a > 0) acc[v][m] += dwx[a] * Pq[v][b];
         }
+    }
     }
     if constexpr (!FP64) {
       // FP32 form: the gravity source (0, -gx drho, -gy drho, -(gx m_x + gy m_y)) is linear
