@@ -757,7 +757,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
           clr[v][b] = s2;
         }
       const float fxf = sfxf[fi];
-      float mom[NV][NQ];
+      float2 mom[2][NQ];  // edge moments of the variable pairs (0, 1) and (2, 3)
 #pragma unroll
       for (int q = 0; q < NQ; ++q) {
         float2 d2[NV];
@@ -772,16 +772,24 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
         }
         eq_point(A, fxf, sfyv[fj * NQ + q], re, pe);
         face_point_pk<0>(A, d2, re, pe, F);
+        const float2 Fp[2] = {make_float2(F[0], F[1]), make_float2(F[2], F[3])};
 #pragma unroll
-        for (int v = 0; v < NV; ++v)
+        for (int pp = 0; pp < 2; ++pp)
 #pragma unroll
-          for (int b = 0; b < NQ; ++b)
-            mom[v][b] = (q == 0 ? 0.f : mom[v][b]) + F[v] * (0.5f * T::BW(b, q));
+          for (int c = 0; c < NQ; ++c) {
+            const float w = 0.5f * T::BW(c, q);
+            mom[pp][c] = __ffma2_rn(Fp[pp], make_float2(w, w), q == 0 ? make_float2(0.f, 0.f) : mom[pp][c]);
+          }
       }
+      const float2 h2 = make_float2(A.hidx, A.hidx);
 #pragma unroll
-      for (int v = 0; v < NV; ++v)
+      for (int pp = 0; pp < 2; ++pp)
 #pragma unroll
-        for (int b = 0; b < NQ; ++b) sfx[(v * NQ + b) * FXS + f] = mom[v][b] * A.hidx;
+        for (int c = 0; c < NQ; ++c) {
+          const float2 r2 = __fmul2_rn(mom[pp][c], h2);
+          sfx[((2 * pp) * NQ + c) * FXS + f] = r2.x;
+          sfx[((2 * pp + 1) * NQ + c) * FXS + f] = r2.y;
+        }
       continue;
     }
     R cl[NV][NQ], cr[NV][NQ];
@@ -855,7 +863,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
           cbt[v][a] = s2;
         }
       const float fyf = sfyf[fj];
-      float mom[NV][NQ];
+      float2 mom[2][NQ];  // edge moments of the variable pairs (0, 1) and (2, 3)
 #pragma unroll
       for (int q = 0; q < NQ; ++q) {
         float2 d2[NV];
@@ -870,16 +878,24 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
         }
         eq_point(A, sfxv[fi * NQ + q], fyf, re, pe);
         face_point_pk<1>(A, d2, re, pe, F);
+        const float2 Fp[2] = {make_float2(F[0], F[1]), make_float2(F[2], F[3])};
 #pragma unroll
-        for (int v = 0; v < NV; ++v)
+        for (int pp = 0; pp < 2; ++pp)
 #pragma unroll
-          for (int a = 0; a < NQ; ++a)
-            mom[v][a] = (q == 0 ? 0.f : mom[v][a]) + F[v] * (0.5f * T::BW(a, q));
+          for (int c = 0; c < NQ; ++c) {
+            const float w = 0.5f * T::BW(c, q);
+            mom[pp][c] = __ffma2_rn(Fp[pp], make_float2(w, w), q == 0 ? make_float2(0.f, 0.f) : mom[pp][c]);
+          }
       }
+      const float2 h2 = make_float2(A.hidy, A.hidy);
 #pragma unroll
-      for (int v = 0; v < NV; ++v)
+      for (int pp = 0; pp < 2; ++pp)
 #pragma unroll
-        for (int a = 0; a < NQ; ++a) sfy[(v * NQ + a) * FYS + f] = mom[v][a] * A.hidy;
+        for (int c = 0; c < NQ; ++c) {
+          const float2 r2 = __fmul2_rn(mom[pp][c], h2);
+          sfy[((2 * pp) * NQ + c) * FYS + f] = r2.x;
+          sfy[((2 * pp + 1) * NQ + c) * FYS + f] = r2.y;
+        }
       continue;
     }
     R cb[NV][NQ], ct[NV][NQ];
