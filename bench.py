@@ -212,6 +212,40 @@ def run_reference(args):
 
 # ---------------------------------------------------------------- our arm
 
+def batch_leg(wb, n, dev, steps=24, warmup=6):
+    """The batched form on n instances: DOF-updates/s over `steps` CFL steps (host clock
+    around graph launches + sync, after `warmup` steps that include the graph capture), and
+    its HBM roofline fraction (20 B per DOF-update per SSP-RK2 step, all stage launches)."""
+    cfgs, ics = wb.batch_workload(n=n, device=dev)
+    with wb.Batch(cfgs) as bt:
+        bt.init_perturbation(ics)
+        bt.step(warmup)
+        bt.sync()
+        t0 = time.perf_counter()
+        bt.step(steps)
+        bt.sync()
+        el = time.perf_counter() - t0
+        dofs = bt.dofs
+    peak, peak_kind = measured_hbm_peak()
+    achieved = BYTES_PER_DOF_UPDATE["fp32"] * dofs * steps / el / 1e9
+    return {"value": dofs * steps / el, "unit": UNIT, "instances": len(cfgs), "dofs": dofs,
+            "steps": steps, "ms_per_step": el / steps * 1e3,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind,
+                         "kernel": "k_batch_stage<float>", "note": "whole step, host clock"},
+            "workload": "%d instances: N = exp(U(ln 32, ln 512)), degree 0..2 (P basis), "
+                        "isothermal or polytrope, Gaussian bump 10^U(-6,-2); FP32, SSP-RK2, "
+                        "CFL steps" % len(cfgs)}
+
+
+def run_batch_only(args):
+    wb = load_package()
+    line = {"metric": "batched form: " + UNIT, "impl": "batch"}
+    line.update(batch_leg(wb, args.batch, 0, steps=args.steps, warmup=max(args.warmup, 6)))
+    print(json.dumps(line))
+    return 0
+
+
 def run_ours(args):
     import torch
     dist, rank, world, lr = dist_init()
@@ -347,21 +381,7 @@ def run_ours(args):
     # the batched form (512 independent instances, one persistent launch per stage, CUDA
     # graph of six steps): reported beside the headline, not part of it
     if rank == 0 and not args.quick:
-        cfgs, ics = wb.batch_workload(n=512, device=dev)
-        with wb.Batch(cfgs) as bt:
-            bt.init_perturbation(ics)
-            bt.step(6)  # eager steps and the graph capture
-            bt.sync()
-            nb = 24
-            t0 = time.perf_counter()
-            bt.step(nb)
-            bt.sync()
-            el = time.perf_counter() - t0
-            extra["batch"] = {"value": bt.dofs * nb / el, "unit": UNIT, "instances": len(cfgs),
-                              "dofs": bt.dofs, "steps": nb,
-                              "workload": "512 instances: N = exp(U(ln 32, ln 512)), degree "
-                                          "0..2 (P basis), isothermal or polytrope, Gaussian "
-                                          "bump 10^U(-6,-2); FP32, SSP-RK2, CFL steps"}
+        extra["batch"] = batch_leg(wb, 512, dev)
 
     cpu = None
     if rank == 0 and not args.quick:
@@ -451,6 +471,8 @@ def main():
     ap.add_argument("--accuracy", action="store_true",
                     help="run the cfg3 accuracy study instead of the benchmark")
     ap.add_argument("--accuracy-steps", type=int, default=500)
+    ap.add_argument("--batch", type=int, default=0,
+                    help="run only the batched form with this many instances (profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -458,6 +480,8 @@ def main():
         return run_reference(args)
     if args.accuracy:
         return run_accuracy(args)
+    if args.batch > 0:
+        return run_batch_only(args)
     return run_ours(args)
 
 

@@ -23,10 +23,12 @@ struct wb_batch {
   std::vector<wb_config> cfgs;
   int device = 0;
   cudaStream_t stream = nullptr;
-  int4 *items = nullptr;
+  int4 *items = nullptr;  // all items, degree 2 first, then 1, then 0
   int nitems = 0;
-  size_t smem = 0;
-  int bufsz = 0;
+  int koff[3] = {0, 0, 0};  // per degree: first item, item count, tile buffer, shared memory
+  int kcount[3] = {0, 0, 0};
+  int kbuf[3] = {0, 0, 0};
+  size_t ksmem[3] = {0, 0, 0};
   int pos = 0;                        // some instance runs the positivity limiter
   StageArgs<float> *args = nullptr;  // [6 phases][2 stages][n]
   const float **state_ptrs = nullptr;  // [6 phases][n] current state per phase
@@ -76,11 +78,16 @@ int build_args(wb_batch *b, int dt_mode, double dt) {
   return WB_OK;
 }
 
+// One launch per degree and stage; every stage-1 launch precedes every stage-2 launch
+// (stream order), and launches of different degrees touch disjoint instances.
 int launch_phase(wb_batch *b, int p) {
   const int n = (int)b->inst.size();
   int grid = 0;
-  BCK(launch_batch_stage(b->args + ((size_t)p * 2 + 0) * n, b->items, b->nitems, b->bufsz, b->smem, b->pos, &grid, b->stream));
-  BCK(launch_batch_stage(b->args + ((size_t)p * 2 + 1) * n, b->items, b->nitems, b->bufsz, b->smem, b->pos, &grid, b->stream));
+  for (int st = 0; st < 2; ++st)
+    for (int K = 2; K >= 0; --K)
+      if (b->kcount[K] > 0)
+        BCK(launch_batch_stage(b->args + ((size_t)p * 2 + st) * n, b->items + b->koff[K],
+                               b->kcount[K], b->kbuf[K], b->ksmem[K], b->pos, K, &grid, b->stream));
   return WB_OK;
 }
 
@@ -137,8 +144,8 @@ int wb_batch_create(const wb_config *cfgs, int32_t n, wb_batch **out) {
   BCK(cudaSetDevice(b->device));
   BCK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
   std::vector<int4> items;
-  int bufmax = 0;
-  size_t fluxmax = 0;
+  int bufmax[3] = {0, 0, 0};
+  size_t fluxmax[3] = {0, 0, 0};
   for (int i = 0; i < n; ++i) {
     wb_config c = cfgs[i];
     if (c.tile_x <= 0) {
@@ -161,16 +168,23 @@ int wb_batch_create(const wb_config *cfgs, int32_t n, wb_batch **out) {
         items.push_back(make_int4(i, i0, j0, (c.order << 24) | (tx << 12) | ty));
     const TileLayout L = tile_layout(c.order, WB_BASIS_P, tx, ty, c.limiter == 1 && c.order >= 1);
     if (c.limiter == 2 && c.order >= 1) b->pos = 1;
-    bufmax = std::max(bufmax, L.buf);
-    fluxmax = std::max(fluxmax, (size_t)NV * (c.order + 1) * ((size_t)ty * (tx + 1) + (size_t)(ty + 1) * tx));
+    const int K = c.order;
+    bufmax[K] = std::max(bufmax[K], L.buf);
+    fluxmax[K] = std::max(fluxmax[K], (size_t)NV * (K + 1) * ((size_t)ty * (tx + 1) + (size_t)(ty + 1) * tx));
   }
-  // costlier (higher-degree) tiles first so the static stride balances better
+  // one contiguous range per degree (2, 1, 0), each launched by its own kernel
   std::stable_sort(items.begin(), items.end(), [](const int4 &a, const int4 &c) {
     return (a.w >> 24) > (c.w >> 24);
   });
   b->nitems = (int)items.size();
-  b->bufsz = bufmax;
-  b->smem = 64 * sizeof(double) + (2 * (size_t)bufmax + fluxmax) * sizeof(float);
+  for (const int4 &w : items) b->kcount[(w.w >> 24) & 0xff]++;
+  b->koff[2] = 0;
+  b->koff[1] = b->kcount[2];
+  b->koff[0] = b->kcount[2] + b->kcount[1];
+  for (int K = 0; K < 3; ++K) {
+    b->kbuf[K] = bufmax[K];
+    b->ksmem[K] = 64 * sizeof(double) + (2 * (size_t)bufmax[K] + fluxmax[K]) * sizeof(float);
+  }
   BCK(cudaMalloc(&b->items, items.size() * sizeof(int4)));
   BCK(cudaMemcpy(b->items, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice));
   BCK(cudaMalloc(&b->args, (size_t)6 * 2 * n * sizeof(StageArgs<float>)));

@@ -17,27 +17,29 @@ __device__ __forceinline__ void unpack_item(int4 w, int &K, int &TX, int &TY) {
 // The batch runs one tile shape (all instances, all degrees).
 constexpr int BATCH_TX = 32, BATCH_TY = 8;
 
-// Stage the item `it` (instance arguments copied to sA, tile staged into buf).
-template <typename R>
+// Stage the item `w` of degree K (instance arguments copied to sA, tile staged into buf).
+template <typename R, int K>
 __device__ __forceinline__ void item_load(const StageArgs<R> *__restrict__ args, const int4 w,
                                           StageArgs<R> &sA, R *buf, int tid, int nthr) {
   static_assert(sizeof(StageArgs<R>) % 4 == 0, "word copy");
   const int *src = reinterpret_cast<const int *>(args + w.x);
   for (int k = tid; k < (int)(sizeof(StageArgs<R>) / 4); k += nthr)
     reinterpret_cast<int *>(&sA)[k] = src[k];
-  int K, TX, TY;
-  unpack_item(w, K, TX, TY);
   const StageArgs<R> &A = args[w.x];
   const bool lim = A.limiter == 1 && A.lim_y && K >= 1;
-  if (K == 0) tile_load_async<R, 0, 1, BATCH_TX, BATCH_TY>(A, lim, w.y, w.z, buf, tid);
-  else if (K == 1) tile_load_async<R, 1, 1, BATCH_TX, BATCH_TY>(A, lim, w.y, w.z, buf, tid);
-  else tile_load_async<R, 2, 1, BATCH_TX, BATCH_TY>(A, lim, w.y, w.z, buf, tid);
+  tile_load_async<R, K, 1, BATCH_TX, BATCH_TY>(A, lim, w.y, w.z, buf, tid);
 }
 
-// Persistent batched stage: CTAs stride over the work list; the next item is staged
-// (cp.async) while the current one is computed.  bufsz = the largest tile buffer.
-template <typename R, bool POS>
-__global__ void __launch_bounds__(256, 2)
+// Resident CTAs per SM the degree-K batch kernel is compiled for (register budget
+// 65536 / (256 x this)); its shared memory (two staged tiles + the face fluxes) allows it.
+__host__ __device__ constexpr int batch_min_blocks(int K) { return K == 0 ? 4 : K == 1 ? 3 : 2; }
+
+// Persistent batched stage for the items of degree K: CTAs stride over the work list; the
+// next item is staged (cp.async) while the current one is computed.  bufsz = the largest
+// tile buffer of the degree.  One kernel per degree gives each its own register budget
+// (and occupancy) and no runtime dispatch on K.
+template <typename R, int K, bool POS>
+__global__ void __launch_bounds__(256, batch_min_blocks(K))
     k_batch_stage(const StageArgs<R> *__restrict__ args, const int4 *__restrict__ items, int nitems,
                   int bufsz) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -50,17 +52,15 @@ __global__ void __launch_bounds__(256, 2)
   // frees the previous item's buffer, argument slot and flux area (as in k_stage).
   const int G = gridDim.x;
   int it = blockIdx.x;
-  if (it < nitems) item_load(args, items[it], sA[0], bufs, tid, nthr);
+  if (it < nitems) item_load<R, K>(args, items[it], sA[0], bufs, tid, nthr);
   cp_async_commit();
   for (int k = 0; it < nitems; it += G, ++k) {
     cp_async_wait<0>();
     __syncthreads();
     if (it + G < nitems)
-      item_load(args, items[it + G], sA[(k + 1) & 1], bufs + ((k + 1) & 1) * bufsz, tid, nthr);
+      item_load<R, K>(args, items[it + G], sA[(k + 1) & 1], bufs + ((k + 1) & 1) * bufsz, tid, nthr);
     cp_async_commit();
     const int4 w = items[it];
-    int K, TX, TY;
-    unpack_item(w, K, TX, TY);
     const StageArgs<R> &A = sA[k & 1];
     R *buf = bufs + (k & 1) * bufsz;
     const double dt = stage_dt(A);
@@ -72,9 +72,8 @@ __global__ void __launch_bounds__(256, 2)
       S->smax[A.parity ^ 1][1] = 0ull;
     }
     const bool lim = A.limiter == 1 && A.lim_y && K >= 1;
-    if (K == 0) tile_compute<R, 0, 1, BATCH_TX, BATCH_TY, POS ? WB_VAR_POSITIVITY : 0>(A, lim, w.y, w.z, buf, flux, red, tid, dt, nullptr, false);
-    else if (K == 1) tile_compute<R, 1, 1, BATCH_TX, BATCH_TY, POS ? WB_VAR_POSITIVITY : 0>(A, lim, w.y, w.z, buf, flux, red, tid, dt, nullptr, false);
-    else tile_compute<R, 2, 1, BATCH_TX, BATCH_TY, POS ? WB_VAR_POSITIVITY : 0>(A, lim, w.y, w.z, buf, flux, red, tid, dt, nullptr, false);
+    tile_compute<R, K, 1, BATCH_TX, BATCH_TY, POS ? WB_VAR_POSITIVITY : 0>(
+        A, lim, w.y, w.z, buf, flux, red, tid, dt, nullptr, false, true);
   }
   cp_async_wait<0>();
 }

@@ -11,29 +11,38 @@ WB_DEFINE_PRECISION_ENTRY_POINTS(float)
 
 namespace wb {
 
-template <bool POS>
+template <int K, bool POS>
 static cudaError_t launch_batch_stage_t(const StageArgs<float> *args, const int4 *items,
                                         int nitems, int bufsz, size_t smem, int *grid_out,
                                         cudaStream_t s) {
-  cudaError_t e = cudaFuncSetAttribute(k_batch_stage<float, POS>,
+  cudaError_t e = cudaFuncSetAttribute(k_batch_stage<float, K, POS>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int dev = 0, nsm = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_stage<float, POS>, 256, smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_stage<float, K, POS>, 256, smem);
   if (e != cudaSuccess) return e;
   int grid = nsm * (per_sm > 0 ? per_sm : 1);
   if (grid > nitems) grid = nitems;
   if (grid_out) *grid_out = grid;
-  k_batch_stage<float, POS><<<grid, 256, smem, s>>>(args, items, nitems, bufsz);
+  k_batch_stage<float, K, POS><<<grid, 256, smem, s>>>(args, items, nitems, bufsz);
   return cudaGetLastError();
 }
 
 cudaError_t launch_batch_stage(const StageArgs<float> *args, const int4 *items, int nitems,
-                               int bufsz, size_t smem, int pos, int *grid_out, cudaStream_t s) {
-  return pos ? launch_batch_stage_t<true>(args, items, nitems, bufsz, smem, grid_out, s)
-             : launch_batch_stage_t<false>(args, items, nitems, bufsz, smem, grid_out, s);
+                               int bufsz, size_t smem, int pos, int K, int *grid_out,
+                               cudaStream_t s) {
+  switch (K) {
+    case 0: return launch_batch_stage_t<0, false>(args, items, nitems, bufsz, smem, grid_out, s);
+    case 1:
+      return pos ? launch_batch_stage_t<1, true>(args, items, nitems, bufsz, smem, grid_out, s)
+                 : launch_batch_stage_t<1, false>(args, items, nitems, bufsz, smem, grid_out, s);
+    case 2:
+      return pos ? launch_batch_stage_t<2, true>(args, items, nitems, bufsz, smem, grid_out, s)
+                 : launch_batch_stage_t<2, false>(args, items, nitems, bufsz, smem, grid_out, s);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 cudaError_t launch_batch_max_speed(const StageArgs<float> *args, const float *const *state,

@@ -665,14 +665,17 @@ __device__ __forceinline__ void tile_load_async(const StageArgs<R> &A, const boo
 }
 
 // Compute one staged tile: limiter, face fluxes, cell quadrature, RK combination and the
-// wave-speed reduction.  Thread tid owns cell (tid % TX, tid / TX).  Ends with a CTA
-// barrier, after which `buf` and the flux area may be reused.
+// wave-speed reduction.  Thread tid owns cell (tid % TX, tid / TX).  With end_sync it ends
+// with a CTA barrier, after which `buf` and the flux area may be reused.  The wave speed
+// goes to speed_acc (the caller reduces later), or by warp atomics (warp_speed), or by a
+// CTA reduction and one atomic.
 template <typename R, int K, int BASIS, int TX, int TY, int VAR>
 __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool lim_,
                                              const int i0, const int j0, R *buf, R *flux,
                                              double *red, const int tid, const double dt,
                                              double *speed_acc = nullptr,
-                                             const bool end_sync = true) {
+                                             const bool end_sync = true,
+                                             const bool warp_speed = false) {
   constexpr int NQ = K + 1;
   constexpr int NB = num_modes(K, BASIS);
   constexpr bool FP64 = std::is_same<R, double>::value;
@@ -1230,6 +1233,16 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
     if (speed_acc) {  // the caller reduces once after its last tile
       speed_acc[0] = fmax(speed_acc[0], spx);
       speed_acc[1] = fmax(speed_acc[1], spy);
+    } else if (warp_speed) {  // one atomic per warp and no CTA barrier (batched form)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        spx = fmax(spx, __shfl_xor_sync(0xffffffffu, spx, o));
+        spy = fmax(spy, __shfl_xor_sync(0xffffffffu, spy, o));
+      }
+      if ((tid & 31) == 0) {
+        atomicMax(&A.dev->smax[A.parity ^ 1][0], (unsigned long long)__double_as_longlong(spx));
+        atomicMax(&A.dev->smax[A.parity ^ 1][1], (unsigned long long)__double_as_longlong(spy));
+      }
     } else {
       double mx = block_max(spx, red, tid, nthr);
       double my = block_max(spy, red, tid, nthr);
