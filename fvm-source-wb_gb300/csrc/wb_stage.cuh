@@ -80,6 +80,13 @@ __device__ __forceinline__ R gminmod(R x, R y, R z, R Mh2) {
   return minmod3(x, y, z);
 }
 
+// s^n for the polytropic equilibrium.  FP32 form: the fast intrinsic (MUFU exp2/log2,
+// about 1e-7 relative), against an accurate powf that costs tens of instructions at every
+// quadrature point.  The equilibrium values enter the FP32 form only as coefficients of
+// perturbation terms, so this is far inside its 1e-6 budget; FP64 stays IEEE.
+__device__ __forceinline__ float eq_pow(float s, float n) { return __powf(s, n); }
+__device__ __forceinline__ double eq_pow(double s, double n) { return pow(s, n); }
+
 // Equilibrium density/pressure from the separable factors (see wb_tables.cpp).
 template <typename R>
 __device__ __forceinline__ void eq_point(const StageArgs<R> &A, R fx, R fy, R &re, R &pe) {
@@ -89,7 +96,7 @@ __device__ __forceinline__ void eq_point(const StageArgs<R> &A, R fx, R fy, R &r
     pe = A.p0 * t;
   } else if (A.eq_kind == 2) {
     R s = fx + fy;
-    re = pow(s, A.npoly);
+    re = eq_pow(s, A.npoly);
     pe = A.kpoly * (re * s);
   } else {
     re = R(0);
