@@ -594,7 +594,11 @@ __device__ __forceinline__ void tile_load_async(const StageArgs<R> &A, const boo
   constexpr int CPR = PX / VEC;             // chunks per stored row
   // x-interior tile with 16-byte aligned rows: copy [i0-4, i0+TX+4) of every row in
   // 16-byte chunks (rows still BC-mapped in y); otherwise element-wise with x mapping
-  const bool vec = i0 >= 4 && i0 + TX + 4 <= nx && (nx % VEC) == 0;
+  const bool xin = i0 >= 4 && i0 + TX + 4 <= nx;
+  const bool vec = xin && (nx % VEC) == 0;
+  // rows only 8-byte aligned (FP32, nx even but not a multiple of 4): 8-byte chunks
+  constexpr int VEC2 = 8 / (int)sizeof(R), CPR2 = PX / (VEC2 > 0 ? VEC2 : 1);
+  const bool vec2 = VEC2 == 2 && xin && (nx % 2) == 0 && (P % 2) == 0;
   const int nrow = NV * L.NB * L.RY;
   if (!modes) {
     // the modes come by TMA (k_stage)
@@ -605,6 +609,14 @@ __device__ __forceinline__ void tile_load_async(const StageArgs<R> &A, const boo
       const int gj = wrap_index(j0 + ry - 1, ny, A.bc_y);
       cp_async<16>(buf + L.su + row * PX + ch * VEC,
                    A.x + pl * P + (long long)gj * nx + (i0 - 4) + ch * VEC);
+    }
+  } else if (vec2) {
+    for (int k = tid; k < nrow * CPR2; k += nthr) {
+      const int row = k / CPR2, ch = k - row * CPR2;
+      const int pl = row / L.RY, ry = row - pl * L.RY;
+      const int gj = wrap_index(j0 + ry - 1, ny, A.bc_y);
+      cp_async<8>(buf + L.su + row * PX + ch * 2,
+                  A.x + pl * P + (long long)gj * nx + (i0 - 4) + ch * 2);
     }
   } else {
     int gc[3];
