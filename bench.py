@@ -219,6 +219,7 @@ def batch_leg(wb, n, dev, steps=24, warmup=6):
     cfgs, ics = wb.batch_workload(n=n, device=dev)
     with wb.Batch(cfgs) as bt:
         bt.init_perturbation(ics)
+        tiles = bt.autotune(3)
         bt.step(warmup)
         bt.sync()
         t0 = time.perf_counter()
@@ -230,6 +231,8 @@ def batch_leg(wb, n, dev, steps=24, warmup=6):
     achieved = BYTES_PER_DOF_UPDATE["fp32"] * dofs * steps / el / 1e9
     return {"value": dofs * steps / el, "unit": UNIT, "instances": len(cfgs), "dofs": dofs,
             "steps": steps, "ms_per_step": el / steps * 1e3,
+            "tiles": {"K%d_%s" % (k, "small" if c == 0 else "large"): "%dx%d" % t
+                      for (k, c), t in sorted(tiles.items())},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
                          "kernel": "k_batch_stage<float>", "note": "whole step, host clock"},

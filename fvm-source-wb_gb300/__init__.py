@@ -94,7 +94,7 @@ def lib():
             "wb_batch_last_error": ([p], ctypes.c_char_p),
             "wb_batch_init_perturbation": ([p, p], i32), "wb_batch_step": ([p, i32, d], i32),
             "wb_batch_sync": ([p], i32), "wb_batch_download": ([p, i32, p], i32),
-            "wb_batch_total_dofs": ([p, p], i32),
+            "wb_batch_total_dofs": ([p, p], i32), "wb_batch_autotune": ([p, i32, p], i32),
             "wb1d_create": ([p, p], i32), "wb1d_destroy": ([p], i32),
             "wb1d_last_error": ([p], ctypes.c_char_p), "wb1d_upload": ([p, p], i32),
             "wb1d_download": ([p, p], i32), "wb1d_compute_update": ([p, p, p], i32),
@@ -548,6 +548,14 @@ class Batch:
 
     def step(self, nsteps=1, dt=-1.0):
         self._check(lib().wb_batch_step(self._b, int(nsteps), float(dt)))
+
+    def autotune(self, reps=3):
+        """Pick the tile shape of every (degree, size class) group by timing; returns
+        {(degree, size_class): (TX, TY)} (size class 0: max(nx, ny) < 128)."""
+        t = np.zeros(12, dtype=np.int32)
+        self._check(lib().wb_batch_autotune(self._b, int(reps), _ptr(t)))
+        return {(k, c): (int(t[(2 * k + c) * 2]), int(t[(2 * k + c) * 2 + 1]))
+                for k in range(3) for c in range(2)}
 
     def sync(self):
         self._check(lib().wb_batch_sync(self._b))

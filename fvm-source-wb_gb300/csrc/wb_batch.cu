@@ -23,12 +23,18 @@ struct wb_batch {
   std::vector<wb_config> cfgs;
   int device = 0;
   cudaStream_t stream = nullptr;
-  int4 *items = nullptr;  // all items, degree 2 first, then 1, then 0
+  int4 *items = nullptr;  // all items, one contiguous range per group
   int nitems = 0;
-  int koff[3] = {0, 0, 0};  // per degree: first item, item count, tile buffer, shared memory
-  int kcount[3] = {0, 0, 0};
-  int kbuf[3] = {0, 0, 0};
-  size_t ksmem[3] = {0, 0, 0};
+  size_t items_cap = 0;
+  // A group = the items of one degree K on one tile shape, launched by its own kernel.
+  struct Group {
+    int K, TX, TY, off, count, buf;
+    size_t smem;
+  };
+  std::vector<Group> groups;
+  // Tile of each instance: pinned by its config, or the choice for its (degree, size class)
+  std::vector<int> pin_tx, pin_ty, size_class;
+  int choice[3][2][2] = {{{32, 8}, {32, 8}}, {{32, 8}, {32, 8}}, {{32, 8}, {32, 8}}};
   int pos = 0;                        // some instance runs the positivity limiter
   StageArgs<float> *args = nullptr;  // [6 phases][2 stages][n]
   const float **state_ptrs = nullptr;  // [6 phases][n] current state per phase
@@ -78,16 +84,98 @@ int build_args(wb_batch *b, int dt_mode, double dt) {
   return WB_OK;
 }
 
-// One launch per degree and stage; every stage-1 launch precedes every stage-2 launch
-// (stream order), and launches of different degrees touch disjoint instances.
+// One launch per group and stage; every stage-1 launch precedes every stage-2 launch
+// (stream order), and launches of different groups touch disjoint instances.
 int launch_phase(wb_batch *b, int p) {
   const int n = (int)b->inst.size();
   int grid = 0;
   for (int st = 0; st < 2; ++st)
-    for (int K = 2; K >= 0; --K)
-      if (b->kcount[K] > 0)
-        BCK(launch_batch_stage(b->args + ((size_t)p * 2 + st) * n, b->items + b->koff[K],
-                               b->kcount[K], b->kbuf[K], b->ksmem[K], b->pos, K, &grid, b->stream));
+    for (const wb_batch::Group &g : b->groups)
+      BCK(launch_batch_stage(b->args + ((size_t)p * 2 + st) * n, b->items + g.off, g.count, g.buf,
+                             g.smem, b->pos, g.K, g.TX, g.TY, &grid, b->stream));
+  return WB_OK;
+}
+
+// Size class of an instance for the tile choice: small grids (side < 128) and the rest.
+int size_class_of(const wb_config &c) { return std::max(c.nx, c.ny) < 128 ? 0 : 1; }
+
+void instance_tile(const wb_batch *b, int i, int *tx, int *ty) {
+  if (b->pin_tx[i] > 0) {
+    *tx = b->pin_tx[i];
+    *ty = b->pin_ty[i];
+  } else {
+    const int *t = b->choice[b->cfgs[i].order][b->size_class[i]];
+    *tx = t[0];
+    *ty = t[1];
+  }
+}
+
+// Items and groups of the instances `sel` (each on tile instance_tile, or on tx x ty when
+// given), appended to items / groups.
+void make_items(const wb_batch *b, const std::vector<int> &sel, int ftx, int fty,
+                std::vector<int4> &items, std::vector<wb_batch::Group> &groups) {
+  struct Key {
+    int K, TX, TY, i;
+  };
+  std::vector<Key> keys;
+  for (int i : sel) {
+    int tx = ftx, ty = fty;
+    if (tx <= 0) instance_tile(b, i, &tx, &ty);
+    keys.push_back({b->cfgs[i].order, tx, ty, i});
+  }
+  // degree 2 first (the costliest launches start first), then by tile shape
+  std::stable_sort(keys.begin(), keys.end(), [](const Key &x, const Key &y) {
+    return x.K != y.K ? x.K > y.K : (x.TX != y.TX ? x.TX > y.TX : x.TY < y.TY);
+  });
+  for (size_t k = 0; k < keys.size(); ++k) {
+    const Key &q = keys[k];
+    const wb_config &c = b->cfgs[q.i];
+    if (groups.empty() || groups.back().K != q.K || groups.back().TX != q.TX ||
+        groups.back().TY != q.TY)
+      groups.push_back({q.K, q.TX, q.TY, (int)items.size(), 0, 0, 0});
+    wb_batch::Group &g = groups.back();
+    for (int j0 = 0; j0 < c.ny; j0 += q.TY)
+      for (int i0 = 0; i0 < c.nx; i0 += q.TX) {
+        items.push_back(make_int4(q.i, i0, j0, (q.K << 24) | (q.TX << 12) | q.TY));
+        ++g.count;
+      }
+    const TileLayout L = tile_layout(q.K, WB_BASIS_P, q.TX, q.TY, c.limiter == 1 && q.K >= 1);
+    g.buf = std::max(g.buf, L.buf);
+    const size_t flux = (size_t)NV * (q.K + 1) * ((size_t)q.TY * (q.TX + 1) + (size_t)(q.TY + 1) * q.TX);
+    g.smem = std::max(g.smem, 64 * sizeof(double) + (2 * (size_t)g.buf + flux) * sizeof(float));
+  }
+}
+
+// Upload items to b->items (grown as needed).
+int upload_items(wb_batch *b, const std::vector<int4> &items) {
+  if (items.size() > b->items_cap) {
+    cudaFree(b->items);
+    b->items = nullptr;
+    b->items_cap = 0;
+    BCK(cudaMalloc(&b->items, items.size() * sizeof(int4)));
+    b->items_cap = items.size();
+  }
+  BCK(cudaMemcpyAsync(b->items, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice,
+                      b->stream));
+  BCK(cudaStreamSynchronize(b->stream));
+  return WB_OK;
+}
+
+// The work list of the current tile choices (the graph, which holds the old list, goes).
+int build_worklist(wb_batch *b) {
+  std::vector<int> all(b->inst.size());
+  for (size_t i = 0; i < all.size(); ++i) all[i] = (int)i;
+  std::vector<int4> items;
+  std::vector<wb_batch::Group> groups;
+  make_items(b, all, 0, 0, items, groups);
+  int rc = upload_items(b, items);
+  if (rc) return rc;
+  b->nitems = (int)items.size();
+  b->groups = groups;
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
   return WB_OK;
 }
 
@@ -136,19 +224,19 @@ int wb_batch_create(const wb_config *cfgs, int32_t n, wb_batch **out) {
         c.basis != WB_BASIS_P)
       return berr(b, WB_ERR_CONFIG,
                   "batch instances must be FP32-perturbation, SSP-RK2, total-degree basis, one device");
-    if (c.tile_x > 0 && (c.tile_x != 32 || c.tile_y != 8))
-      return berr(b, WB_ERR_CONFIG, "the batch runs 32x8 tiles");
+    if (c.tile_x > 0 && !batch_tile_supported(c.tile_x, c.tile_y))
+      return berr(b, WB_ERR_CONFIG, "batch tiles are 32x8 or 16x16 (or 0: chosen by the batch)");
     if (c.riemann != WB_RIEMANN_LLF)
       return berr(b, WB_ERR_CONFIG, "the batch runs the LLF flux");
   }
   BCK(cudaSetDevice(b->device));
   BCK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
-  std::vector<int4> items;
-  int bufmax[3] = {0, 0, 0};
-  size_t fluxmax[3] = {0, 0, 0};
   for (int i = 0; i < n; ++i) {
     wb_config c = cfgs[i];
-    if (c.tile_x <= 0) {
+    b->pin_tx.push_back(c.tile_x > 0 ? c.tile_x : 0);
+    b->pin_ty.push_back(c.tile_x > 0 ? c.tile_y : 0);
+    b->size_class.push_back(size_class_of(c));
+    if (c.tile_x <= 0) {  // the instance context's own tile is not used by the batch
       c.tile_x = 32;
       c.tile_y = 8;
     }
@@ -161,32 +249,10 @@ int wb_batch_create(const wb_config *cfgs, int32_t n, wb_batch **out) {
     }
     b->inst.push_back(ctx);
     b->cfgs.push_back(c);
-    int tx, ty;
-    ctx_tile(ctx, &tx, &ty);
-    for (int j0 = 0; j0 < c.ny; j0 += ty)
-      for (int i0 = 0; i0 < c.nx; i0 += tx)
-        items.push_back(make_int4(i, i0, j0, (c.order << 24) | (tx << 12) | ty));
-    const TileLayout L = tile_layout(c.order, WB_BASIS_P, tx, ty, c.limiter == 1 && c.order >= 1);
     if (c.limiter == 2 && c.order >= 1) b->pos = 1;
-    const int K = c.order;
-    bufmax[K] = std::max(bufmax[K], L.buf);
-    fluxmax[K] = std::max(fluxmax[K], (size_t)NV * (K + 1) * ((size_t)ty * (tx + 1) + (size_t)(ty + 1) * tx));
   }
-  // one contiguous range per degree (2, 1, 0), each launched by its own kernel
-  std::stable_sort(items.begin(), items.end(), [](const int4 &a, const int4 &c) {
-    return (a.w >> 24) > (c.w >> 24);
-  });
-  b->nitems = (int)items.size();
-  for (const int4 &w : items) b->kcount[(w.w >> 24) & 0xff]++;
-  b->koff[2] = 0;
-  b->koff[1] = b->kcount[2];
-  b->koff[0] = b->kcount[2] + b->kcount[1];
-  for (int K = 0; K < 3; ++K) {
-    b->kbuf[K] = bufmax[K];
-    b->ksmem[K] = 64 * sizeof(double) + (2 * (size_t)bufmax[K] + fluxmax[K]) * sizeof(float);
-  }
-  BCK(cudaMalloc(&b->items, items.size() * sizeof(int4)));
-  BCK(cudaMemcpy(b->items, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice));
+  int rc = build_worklist(b);
+  if (rc) return rc;
   BCK(cudaMalloc(&b->args, (size_t)6 * 2 * n * sizeof(StageArgs<float>)));
   BCK(cudaMalloc(&b->state_ptrs, (size_t)6 * n * sizeof(float *)));
   return build_args(b, 1, 0.0);
@@ -241,6 +307,67 @@ int wb_batch_step(wb_batch *b, int32_t nsteps, double dt) {
     --left;
   }
   for (wb_ctx *c : b->inst) ctx_set_speed_valid(c, true);
+  return WB_OK;
+}
+
+int wb_batch_autotune(wb_batch *b, int32_t reps, int32_t *tiles) {
+  if (!b || reps < 1) return WB_ERR_ARG;
+  BCK(cudaSetDevice(b->device));
+  int rc = ensure_batch_speed(b);
+  if (rc) return rc;
+  const int n = (int)b->inst.size();
+  // Candidates are timed on stage-1 launches of the current phase.  Stage 1 writes only
+  // the buffer its real launch overwrites next and the next-parity time and speed slots,
+  // which that launch rewrites too, so the instances' states are not changed.
+  const StageArgs<float> *a1 = b->args + ((size_t)b->phase * 2 + 0) * n;
+  static const int cand[2][2] = {{32, 8}, {16, 16}};
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  BCK(cudaEventCreate(&e0));
+  BCK(cudaEventCreate(&e1));
+  rc = WB_OK;
+  for (int K = 0; K < 3 && !rc; ++K)
+    for (int cls = 0; cls < 2 && !rc; ++cls) {
+      std::vector<int> sel;
+      for (int i = 0; i < n; ++i)
+        if (b->pin_tx[i] == 0 && b->cfgs[i].order == K && b->size_class[i] == cls) sel.push_back(i);
+      if (sel.empty()) continue;
+      float best = 0.f;
+      for (int c = 0; c < 2 && !rc; ++c) {
+        std::vector<int4> items;
+        std::vector<wb_batch::Group> groups;
+        make_items(b, sel, cand[c][0], cand[c][1], items, groups);
+        if ((rc = upload_items(b, items))) break;
+        float ms = 0.f;
+        for (int r = 0; r <= reps && !rc; ++r) {  // launch 0 warms up
+          if (r == 1 && cudaEventRecord(e0, b->stream) != cudaSuccess) rc = WB_ERR_CUDA;
+          for (const wb_batch::Group &g : groups)
+            if (!rc && launch_batch_stage(a1, b->items + g.off, g.count, g.buf, g.smem, b->pos,
+                                          g.K, g.TX, g.TY, nullptr, b->stream) != cudaSuccess)
+              rc = berr(b, WB_ERR_CUDA, "autotune launch failed");
+        }
+        if (rc) break;
+        if (cudaEventRecord(e1, b->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+            cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+          rc = berr(b, WB_ERR_CUDA, "autotune timing failed");
+          break;
+        }
+        if (c == 0 || ms < best) {
+          best = ms;
+          b->choice[K][cls][0] = cand[c][0];
+          b->choice[K][cls][1] = cand[c][1];
+        }
+      }
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  if ((rc = build_worklist(b))) return rc;
+  if (tiles)
+    for (int K = 0; K < 3; ++K)
+      for (int cls = 0; cls < 2; ++cls) {
+        tiles[(K * 2 + cls) * 2 + 0] = b->choice[K][cls][0];
+        tiles[(K * 2 + cls) * 2 + 1] = b->choice[K][cls][1];
+      }
   return WB_OK;
 }
 

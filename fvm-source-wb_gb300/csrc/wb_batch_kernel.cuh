@@ -14,11 +14,8 @@ __device__ __forceinline__ void unpack_item(int4 w, int &K, int &TX, int &TY) {
   TY = w.w & 0xfff;
 }
 
-// The batch runs one tile shape (all instances, all degrees).
-constexpr int BATCH_TX = 32, BATCH_TY = 8;
-
 // Stage the item `w` of degree K (instance arguments copied to sA, tile staged into buf).
-template <typename R, int K>
+template <typename R, int K, int TX, int TY>
 __device__ __forceinline__ void item_load(const StageArgs<R> *__restrict__ args, const int4 w,
                                           StageArgs<R> &sA, R *buf, int tid, int nthr) {
   static_assert(sizeof(StageArgs<R>) % 4 == 0, "word copy");
@@ -27,19 +24,19 @@ __device__ __forceinline__ void item_load(const StageArgs<R> *__restrict__ args,
     reinterpret_cast<int *>(&sA)[k] = src[k];
   const StageArgs<R> &A = args[w.x];
   const bool lim = A.limiter == 1 && A.lim_y && K >= 1;
-  tile_load_async<R, K, 1, BATCH_TX, BATCH_TY>(A, lim, w.y, w.z, buf, tid);
+  tile_load_async<R, K, 1, TX, TY>(A, lim, w.y, w.z, buf, tid);
 }
 
 // Resident CTAs per SM the degree-K batch kernel is compiled for (register budget
 // 65536 / (256 x this)); its shared memory (two staged tiles + the face fluxes) allows it.
 __host__ __device__ constexpr int batch_min_blocks(int K) { return K == 0 ? 4 : K == 1 ? 3 : 2; }
 
-// Persistent batched stage for the items of degree K: CTAs stride over the work list; the
-// next item is staged (cp.async) while the current one is computed.  bufsz = the largest
-// tile buffer of the degree.  One kernel per degree gives each its own register budget
-// (and occupancy) and no runtime dispatch on K.
-template <typename R, int K, bool POS>
-__global__ void __launch_bounds__(256, batch_min_blocks(K))
+// Persistent batched stage for the items of one group (degree K, TX x TY tiles): CTAs
+// stride over the group's work list; the next item is staged (cp.async) while the
+// current one is computed.  bufsz = the largest tile buffer of the group.  One kernel per
+// degree gives each its own register budget (and occupancy) and no runtime dispatch on K.
+template <typename R, int K, int TX, int TY, bool POS>
+__global__ void __launch_bounds__(TX * TY, batch_min_blocks(K))
     k_batch_stage(const StageArgs<R> *__restrict__ args, const int4 *__restrict__ items, int nitems,
                   int bufsz) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -52,13 +49,13 @@ __global__ void __launch_bounds__(256, batch_min_blocks(K))
   // frees the previous item's buffer, argument slot and flux area (as in k_stage).
   const int G = gridDim.x;
   int it = blockIdx.x;
-  if (it < nitems) item_load<R, K>(args, items[it], sA[0], bufs, tid, nthr);
+  if (it < nitems) item_load<R, K, TX, TY>(args, items[it], sA[0], bufs, tid, nthr);
   cp_async_commit();
   for (int k = 0; it < nitems; it += G, ++k) {
     cp_async_wait<0>();
     __syncthreads();
     if (it + G < nitems)
-      item_load<R, K>(args, items[it + G], sA[(k + 1) & 1], bufs + ((k + 1) & 1) * bufsz, tid, nthr);
+      item_load<R, K, TX, TY>(args, items[it + G], sA[(k + 1) & 1], bufs + ((k + 1) & 1) * bufsz, tid, nthr);
     cp_async_commit();
     const int4 w = items[it];
     const StageArgs<R> &A = sA[k & 1];
@@ -72,7 +69,7 @@ __global__ void __launch_bounds__(256, batch_min_blocks(K))
       S->smax[A.parity ^ 1][1] = 0ull;
     }
     const bool lim = A.limiter == 1 && A.lim_y && K >= 1;
-    tile_compute<R, K, 1, BATCH_TX, BATCH_TY, POS ? WB_VAR_POSITIVITY : 0>(
+    tile_compute<R, K, 1, TX, TY, POS ? WB_VAR_POSITIVITY : 0>(
         A, lim, w.y, w.z, buf, flux, red, tid, dt, nullptr, false, true);
   }
   cp_async_wait<0>();

@@ -53,8 +53,9 @@ cudaError_t launch_f64_to_f32(float *out, const double *in, long long n, cudaStr
 
 // batched form (FP32): persistent stage over a work list; per-instance max speed
 cudaError_t launch_batch_stage(const StageArgs<float> *args, const int4 *items, int nitems,
-                               int bufsz, size_t smem, int pos, int K, int *grid_out,
-                               cudaStream_t s);
+                               int bufsz, size_t smem, int pos, int K, int TX, int TY,
+                               int *grid_out, cudaStream_t s);
+bool batch_tile_supported(int TX, int TY);  // the tile shapes the batch kernels compile
 cudaError_t launch_batch_max_speed(const StageArgs<float> *args, const float *const *state,
                                    const int4 *items, int nitems, cudaStream_t s);
 

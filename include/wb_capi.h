@@ -228,9 +228,11 @@ int wb_write_dat(wb_ctx *ctx, const char *path, int32_t var);
 
 /* --- batched form -------------------------------------------------------------- */
 typedef struct wb_batch wb_batch;
-/* n independent instances (each its own grid, order, basis, equilibrium, limiter),
- * FP32-perturbation form, advanced together: one persistent launch per RK stage over
- * a work list of cell tiles.  All cfgs must share precision, integrator and device. */
+/* n independent instances (each its own grid, order, equilibrium, limiter), total-degree
+ * basis, FP32-perturbation form, SSP-RK2, advanced together: per RK stage one persistent
+ * launch per group (instances of one degree on one tile shape) over a work list of cell
+ * tiles, the step sequence replayed from a CUDA graph.  An instance's tile_x/tile_y pin
+ * its tile (32x8 or 16x16); 0 leaves it to the batch (32x8 until wb_batch_autotune). */
 int wb_batch_create(const wb_config *cfgs, int32_t n, wb_batch **out);
 int wb_batch_destroy(wb_batch *b);
 const char *wb_batch_last_error(const wb_batch *b);
@@ -238,6 +240,12 @@ int wb_batch_init_perturbation(wb_batch *b, const wb_perturbation *ics);
 /* nsteps steps; each instance takes its own CFL dt (dt <= 0) or the fixed dt */
 int wb_batch_step(wb_batch *b, int32_t nsteps, double dt);
 int wb_batch_sync(wb_batch *b);
+/* Tile autotuner of the batched form: for every (degree, size class) group of instances
+ * without a pinned tile -- size class 0: max(nx, ny) < 128, 1: the rest -- times `reps`
+ * stage launches of each tile shape (32x8, 16x16) on those instances and keeps the
+ * fastest.  The instances' states are not changed.  tiles (optional, int32[12]) receives
+ * the choice (TX, TY) for degree K and class s at [(2K + s) * 2]. */
+int wb_batch_autotune(wb_batch *b, int32_t reps, int32_t *tiles);
 int wb_batch_download(wb_batch *b, int32_t index, double *delta);
 int wb_batch_total_dofs(wb_batch *b, int64_t *dofs);
 

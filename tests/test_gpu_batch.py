@@ -43,3 +43,33 @@ def test_batch_rejects_mixed_precision(wb):
     with pytest.raises(wb.WbError) as ei:
         wb.Batch(cfgs)
     assert ei.value.status == wb.WB_ERR_CONFIG
+
+
+def test_batch_autotune_and_pinned_tiles_keep_results(wb):
+    """wb_batch_autotune changes no state and only regroups the work list: instances on
+    either tile shape (chosen or pinned by the config) still advance exactly as alone."""
+    cfgs, ics = wb.batch_workload(n=10, seed_base=91, nmin=24, nmax=200)
+    cfgs[3].tile_x, cfgs[3].tile_y = 16, 16   # pinned
+    with wb.Batch(cfgs) as b:
+        b.init_perturbation(ics)
+        b.step(2)
+        tiles = b.autotune(2)
+        assert set(tiles.values()) <= {(32, 8), (16, 16)}
+        b.step(8)
+        b.autotune(1)
+        b.step(3)
+        b.sync()
+        outs = [b.download(i) for i in range(len(cfgs))]
+    for i, (c, ic) in enumerate(zip(cfgs, ics)):
+        with wb.Solver(config=c) as s:
+            s.init_perturbation(ic)
+            s.step(13)
+            np.testing.assert_array_equal(outs[i], s.download(), err_msg="instance %d" % i)
+
+
+def test_batch_rejects_unsupported_tile(wb):
+    cfgs, _ = wb.batch_workload(n=2, nmin=16, nmax=20)
+    cfgs[0].tile_x, cfgs[0].tile_y = 16, 8
+    with pytest.raises(wb.WbError) as ei:
+        wb.Batch(cfgs)
+    assert ei.value.status == wb.WB_ERR_CONFIG
