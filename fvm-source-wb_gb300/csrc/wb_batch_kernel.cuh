@@ -17,12 +17,15 @@ __device__ __forceinline__ void unpack_item(int4 w, int &K, int &TX, int &TY) {
 // Stage the item `w` of degree K (instance arguments copied to sA, tile staged into buf).
 template <typename R, int K, int TX, int TY>
 __device__ __forceinline__ void item_load(const StageArgs<R> *__restrict__ args, const int4 w,
-                                          StageArgs<R> &sA, R *buf, int tid, int nthr) {
+                                          StageArgs<R> &sA, double &sdt, R *buf, int tid,
+                                          int nthr) {
   static_assert(sizeof(StageArgs<R>) % 4 == 0, "word copy");
   const int *src = reinterpret_cast<const int *>(args + w.x);
   for (int k = tid; k < (int)(sizeof(StageArgs<R>) / 4); k += nthr)
     reinterpret_cast<int *>(&sA)[k] = src[k];
   const StageArgs<R> &A = args[w.x];
+  // the item's time step, once per item (FP64 divisions are slow on this part)
+  if (tid == 0) sdt = stage_dt(A);
   const bool lim = A.limiter == 1 && A.lim_y && K >= 1;
   tile_load_async<R, K, 1, TX, TY>(A, lim, w.y, w.z, buf, tid);
 }
@@ -41,6 +44,7 @@ __global__ void __launch_bounds__(TX * TY, batch_min_blocks(K))
                   int bufsz) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ __align__(16) StageArgs<R> sA[2];  // instance arguments of the staged items
+  __shared__ double sdt[2];                     // and their time steps
   const int tid = threadIdx.x, nthr = blockDim.x;
   double *red = reinterpret_cast<double *>(smem_raw);
   R *bufs = reinterpret_cast<R *>(smem_raw + 64 * sizeof(double));
@@ -49,18 +53,19 @@ __global__ void __launch_bounds__(TX * TY, batch_min_blocks(K))
   // frees the previous item's buffer, argument slot and flux area (as in k_stage).
   const int G = gridDim.x;
   int it = blockIdx.x;
-  if (it < nitems) item_load<R, K, TX, TY>(args, items[it], sA[0], bufs, tid, nthr);
+  if (it < nitems) item_load<R, K, TX, TY>(args, items[it], sA[0], sdt[0], bufs, tid, nthr);
   cp_async_commit();
   for (int k = 0; it < nitems; it += G, ++k) {
     cp_async_wait<0>();
     __syncthreads();
     if (it + G < nitems)
-      item_load<R, K, TX, TY>(args, items[it + G], sA[(k + 1) & 1], bufs + ((k + 1) & 1) * bufsz, tid, nthr);
+      item_load<R, K, TX, TY>(args, items[it + G], sA[(k + 1) & 1], sdt[(k + 1) & 1],
+                              bufs + ((k + 1) & 1) * bufsz, tid, nthr);
     cp_async_commit();
     const int4 w = items[it];
     const StageArgs<R> &A = sA[k & 1];
     R *buf = bufs + (k & 1) * bufsz;
-    const double dt = stage_dt(A);
+    const double dt = sdt[k & 1];
     if (A.advance_time && w.y == 0 && w.z == 0 && tid == 0) {
       DevState *S = A.dev;
       S->t[A.parity ^ 1] = S->t[A.parity] + dt;

@@ -692,7 +692,7 @@ template <typename R, int K, int BASIS, int TX, int TY, int VAR>
 __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool lim_,
                                              const int i0, const int j0, R *buf, R *flux,
                                              double *red, const int tid, const double dt,
-                                             double *speed_acc = nullptr,
+                                             R *speed_acc = nullptr,
                                              const bool end_sync = true,
                                              const bool warp_speed = false) {
   constexpr int NQ = K + 1;
@@ -972,7 +972,9 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
   const int tx = tid % TX, ty = tid / TX;
   const int gi = i0 + tx, gj = j0 + ty;
   const bool active = gi < nx && gj < ny;
-  double spx = 0.0, spy = 0.0;
+  // wave-speed maxima in the kernel's precision (a maximum of floats is exact; FP64
+  // arithmetic is slow on this part), widened to double only for the atomics
+  R spx = R(0), spy = R(0);
   if (active) {
     const R *uc = su + (ty + 1) * RX + (tx + 1);  // mode m of var v at uc[(v*NB+m)*RXY]
     R acc[NV][NB];
@@ -1238,13 +1240,13 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
         else
           p = pbar + A.gm1 * (d3 - R(0.5) * (d1 * vx + d2 * vy));
         R cs = sqrt(A.gamma * rfmax(p, R(1e-10)) / rfmax(rf, R(1e-10)));
-        spx = (double)(fabs(vx) + cs);
-        spy = (double)(fabs(vy) + cs);
+        spx = fabs(vx) + cs;
+        spy = fabs(vy) + cs;
         bool bad = !(r > R(0)) || !(p > R(0)) || !isfinite(spx) || !isfinite(spy);
         if (A.eq_kind == 0) bad = !isfinite(spx) || !isfinite(spy);
         if (bad) atomicOr(&A.dev->err, 1);
-        if (!isfinite(spx)) spx = 0.0;
-        if (!isfinite(spy)) spy = 0.0;
+        if (!isfinite(spx)) spx = R(0);
+        if (!isfinite(spy)) spy = R(0);
       }
     }
   }
@@ -1259,12 +1261,12 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
         spy = fmax(spy, __shfl_xor_sync(0xffffffffu, spy, o));
       }
       if ((tid & 31) == 0) {
-        atomicMax(&A.dev->smax[A.parity ^ 1][0], (unsigned long long)__double_as_longlong(spx));
-        atomicMax(&A.dev->smax[A.parity ^ 1][1], (unsigned long long)__double_as_longlong(spy));
+        atomicMax(&A.dev->smax[A.parity ^ 1][0], (unsigned long long)__double_as_longlong((double)spx));
+        atomicMax(&A.dev->smax[A.parity ^ 1][1], (unsigned long long)__double_as_longlong((double)spy));
       }
     } else {
-      double mx = block_max(spx, red, tid, nthr);
-      double my = block_max(spy, red, tid, nthr);
+      double mx = block_max((double)spx, red, tid, nthr);
+      double my = block_max((double)spy, red, tid, nthr);
       if (tid == 0) {
         atomicMax(&A.dev->smax[A.parity ^ 1][0], (unsigned long long)__double_as_longlong(mx));
         atomicMax(&A.dev->smax[A.parity ^ 1][1], (unsigned long long)__double_as_longlong(my));
@@ -1327,7 +1329,7 @@ __global__ void __launch_bounds__(TX *TY, std::is_same<R, float>::value ? 2 : 1)
     tile_load_async<R, K, BASIS, TX, TY>(A, lim, i0, j0, buf, tid, !tma);
   };
   bool ok = true;
-  double speed[2] = {0.0, 0.0};  // this thread's wave-speed maxima over its tiles
+  R speed[2] = {R(0), R(0)};  // this thread's wave-speed maxima over its tiles
   // Pipeline: tile t is staged while tile t - G is computed.  The barrier after tile t's
   // data arrives also frees tile t - G's buffer and the flux area, so the next tile's
   // copies are issued right after it and tile_compute needs no closing barrier.
@@ -1357,8 +1359,8 @@ __global__ void __launch_bounds__(TX *TY, std::is_same<R, float>::value ? 2 : 1)
   __syncthreads();  // the last tile's readers are done before the reduction reuses `red`
   // wave-speed maxima of all this CTA's tiles: one block reduction per launch
   if (A.compute_speed) {
-    const double mx = block_max(speed[0], red, tid, TX * TY);
-    const double my = block_max(speed[1], red, tid, TX * TY);
+    const double mx = block_max((double)speed[0], red, tid, TX * TY);
+    const double my = block_max((double)speed[1], red, tid, TX * TY);
     if (tid == 0) {
       atomicMax(&A.dev->smax[A.parity ^ 1][0], (unsigned long long)__double_as_longlong(mx));
       atomicMax(&A.dev->smax[A.parity ^ 1][1], (unsigned long long)__double_as_longlong(my));
