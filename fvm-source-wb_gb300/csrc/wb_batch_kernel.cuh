@@ -111,13 +111,10 @@ __global__ void __launch_bounds__(256)
         }
       R d0 = u[(long long)(0 * NB) * A.plane + cell], d1 = u[(long long)(1 * NB) * A.plane + cell];
       R d2 = u[(long long)(2 * NB) * A.plane + cell], d3 = u[(long long)(3 * NB) * A.plane + cell];
-      R rf = rfmax(rbar + d0, R(1.0e-9f));
-      R inv = R(1) / rf;
-      R vx = d1 * inv, vy = d2 * inv;
-      R p = pbar + A.gm1 * (d3 - R(0.5) * (d1 * vx + d2 * vy));
-      R cs = sqrt(A.gamma * rfmax(p, R(1e-10)) / rfmax(rf, R(1e-10)));
-      spx = (double)(fabs(vx) + cs);
-      spy = (double)(fabs(vy) + cs);
+      R r, p, sx, sy;
+      mean_wave_speed(A, rbar, pbar, d0, d1, d2, d3, r, p, sx, sy);
+      spx = (double)sx;
+      spy = (double)sy;
       if (!isfinite(spx) || !isfinite(spy)) {
         atomicOr(&A.dev->err, 1);
         spx = spy = 0.0;

@@ -104,6 +104,30 @@ __device__ __forceinline__ void eq_point(const StageArgs<R> &A, R fx, R fy, R &r
   }
 }
 
+// CFL wave speeds |u| + c and |v| + c of a cell from its mean perturbation d0..d3 and its
+// mean equilibrium (rbar, pbar); r and p are the full mean density and pressure.  The one
+// formula of the stage kernels' maxima and of the set-up kernels (k_max_speed,
+// k_batch_max_speed), so a restart recomputes bit-identical speeds.  FP32 takes the
+// hardware reciprocal and square root (about 1 ulp); FP64 stays IEEE.
+template <typename R>
+__device__ __forceinline__ void mean_wave_speed(const StageArgs<R> &A, R rbar, R pbar, R d0,
+                                                R d1, R d2, R d3, R &r, R &p, R &spx, R &spy) {
+  r = rbar + d0;
+  const R rf = rfmax(r, R(1.0e-9f));
+  const R inv = frcp(rf);
+  const R vx = d1 * inv, vy = d2 * inv;
+  R cs;
+  if constexpr (std::is_same<R, double>::value) {
+    p = A.gm1 * ((pbar * A.igm1 + d3) - R(0.5) * rf * (vx * vx + vy * vy));
+    cs = sqrt(A.gamma * rfmax(p, R(1e-10)) / rfmax(rf, R(1e-10)));
+  } else {
+    p = pbar + A.gm1 * (d3 - R(0.5) * (d1 * vx + d2 * vy));
+    cs = fsqrt_pos(A.gamma * rfmax(p, R(1e-10)) * frcp(rfmax(rf, R(1e-10))));
+  }
+  spx = fabs(vx) + cs;
+  spy = fabs(vy) + cs;
+}
+
 // ---------------------------------------------------------------- FP64 literal
 // compute_primitive / compute_flux_int / get_source of 2d/benchmark_2d_dg.f90:891-963
 // and benchmark_2d.f90:327-350.
@@ -1229,19 +1253,8 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
         }
       if (oi == 0 && A.compute_speed) {
         // wave speed from the new cell mean of the full state
-        R d0 = val[0][0], d1 = val[1][0], d2 = val[2][0], d3 = val[3][0];
-        R r = rbar + d0;
-        R rf = rfmax(r, R(1.0e-9f));
-        R inv = R(1) / rf;
-        R vx = d1 * inv, vy = d2 * inv;
-        R p;
-        if constexpr (std::is_same<R, double>::value)
-          p = A.gm1 * ((pbar * A.igm1 + d3) - R(0.5) * rf * (vx * vx + vy * vy));
-        else
-          p = pbar + A.gm1 * (d3 - R(0.5) * (d1 * vx + d2 * vy));
-        R cs = sqrt(A.gamma * rfmax(p, R(1e-10)) / rfmax(rf, R(1e-10)));
-        spx = fabs(vx) + cs;
-        spy = fabs(vy) + cs;
+        R r, p;
+        mean_wave_speed(A, rbar, pbar, val[0][0], val[1][0], val[2][0], val[3][0], r, p, spx, spy);
         bool bad = !(r > R(0)) || !(p > R(0)) || !isfinite(spx) || !isfinite(spy);
         if (A.eq_kind == 0) bad = !isfinite(spx) || !isfinite(spy);
         if (bad) atomicOr(&A.dev->err, 1);
