@@ -153,57 +153,37 @@ __device__ __forceinline__ void flux_lit(const double *u, const double *w, doubl
   }
 }
 
-// Volume point: split fluxes (unscaled) and, in FP64, the source (scaled by the 0.25 of
-// the assembly).
-template <typename R>
-__device__ __forceinline__ void vol_point(const StageArgs<R> &A, const R *d, R re, R pe, R *Fx,
-                                          R *Fy, R *S) {
-  if constexpr (std::is_same<R, double>::value) {
-    double ue[NV] = {re, 0.0, 0.0, pe * A.igm1}, u[NV], w[NV], we[NV], f[NV], fe[NV];
+// FP64 volume point: split fluxes F(u_eq + d) - F(u_eq) (unscaled) and the source (scaled
+// by the 0.25 of the assembly).  The FP32 form evaluates its volume points on packed pairs
+// inside tile_compute.
+__device__ __forceinline__ void vol_point(const StageArgs<double> &A, const double *d, double re,
+                                          double pe, double *Fx, double *Fy, double *S) {
+  double ue[NV] = {re, 0.0, 0.0, pe * A.igm1}, u[NV], w[NV], we[NV], f[NV], fe[NV];
 #pragma unroll
-    for (int v = 0; v < NV; ++v) u[v] = ue[v] + d[v];
-    prim_lit(u, w, A.gm1);
-    prim_lit(ue, we, A.gm1);
-    flux_lit<0>(u, w, f);
-    flux_lit<0>(ue, we, fe);
+  for (int v = 0; v < NV; ++v) u[v] = ue[v] + d[v];
+  prim_lit(u, w, A.gm1);
+  prim_lit(ue, we, A.gm1);
+  flux_lit<0>(u, w, f);
+  flux_lit<0>(ue, we, fe);
 #pragma unroll
-    for (int v = 0; v < NV; ++v) Fx[v] = f[v] - fe[v];
-    flux_lit<1>(u, w, f);
-    flux_lit<1>(ue, we, fe);
+  for (int v = 0; v < NV; ++v) Fx[v] = f[v] - fe[v];
+  flux_lit<1>(u, w, f);
+  flux_lit<1>(ue, we, fe);
 #pragma unroll
-    for (int v = 0; v < NV; ++v) Fy[v] = f[v] - fe[v];
-    // rounded products (never contracted into the subtraction below): S(u_eq + 0) and
-    // S(u_eq) must round identically so a zero perturbation cancels exactly
-    double s[NV], se[NV];
-    s[0] = 0.0;
-    s[1] = -__dmul_rn(w[0], A.gx);
-    s[2] = -__dmul_rn(w[0], A.gy);
-    s[3] = -__dmul_rn(w[0], __dadd_rn(__dmul_rn(w[1], A.gx), __dmul_rn(w[2], A.gy)));
-    se[0] = 0.0;
-    se[1] = -__dmul_rn(we[0], A.gx);
-    se[2] = -__dmul_rn(we[0], A.gy);
-    se[3] = -__dmul_rn(we[0], __dadd_rn(__dmul_rn(we[1], A.gx), __dmul_rn(we[2], A.gy)));
+  for (int v = 0; v < NV; ++v) Fy[v] = f[v] - fe[v];
+  // rounded products (never contracted into the subtraction below): S(u_eq + 0) and
+  // S(u_eq) must round identically so a zero perturbation cancels exactly
+  double s[NV], se[NV];
+  s[0] = 0.0;
+  s[1] = -__dmul_rn(w[0], A.gx);
+  s[2] = -__dmul_rn(w[0], A.gy);
+  s[3] = -__dmul_rn(w[0], __dadd_rn(__dmul_rn(w[1], A.gx), __dmul_rn(w[2], A.gy)));
+  se[0] = 0.0;
+  se[1] = -__dmul_rn(we[0], A.gx);
+  se[2] = -__dmul_rn(we[0], A.gy);
+  se[3] = -__dmul_rn(we[0], __dadd_rn(__dmul_rn(we[1], A.gx), __dmul_rn(we[2], A.gy)));
 #pragma unroll
-    for (int v = 0; v < NV; ++v) S[v] = (s[v] - se[v]) * 0.25;
-  } else {
-    // exact differences about a static equilibrium (u_eq velocity 0):
-    //   d(rho u) = m_x, d(rho u^2 + p) = m_x^2/rho + dp, d(rho u v) = m_x m_y / rho,
-    //   d(u (E+p)) = u (H_eq + dE + dp), dp = (gamma-1)(dE - |m|^2/(2 rho))
-    R r = rfmax(re + d[0], R(1.0e-9f));
-    R inv = frcp(r);
-    R vx = d[1] * inv, vy = d[2] * inv;
-    R dp = A.gm1 * (d[3] - R(0.5) * (d[1] * vx + d[2] * vy));
-    R H = A.hgam * pe + d[3] + dp;
-    Fx[0] = d[1];
-    Fx[1] = d[1] * vx + dp;
-    Fx[2] = d[2] * vx;
-    Fx[3] = vx * H;
-    Fy[0] = d[2];
-    Fy[1] = d[1] * vy;
-    Fy[2] = d[2] * vy + dp;
-    Fy[3] = vy * H;
-    (void)S;  // the FP32 form takes the (linear) source from the modes, see tile_compute
-  }
+  for (int v = 0; v < NV; ++v) S[v] = (s[v] - se[v]) * 0.25;
 }
 
 // Face point in direction DIR: numerical flux minus the equilibrium flux, F_hat - F(u_eq),
@@ -271,9 +251,11 @@ __device__ __forceinline__ void face_point(const StageArgs<R> &A, const R *dL, c
         F[v] = (0.5 * (fR[v] + fL[v]) + 0.5 * lam * (uL[v] - uR[v])) - fe[v];
     }
   } else {
-    // exact-difference side quantities: r = rho, vn / vt = normal / transverse velocity,
-    // dp = pressure perturbation, H = E + p of the full state, f = flux difference
-    R fL[NV], fR[NV], lamL, lamR, rs[2], vns[2], vts[2], dps[2], Hs[2], cs[2];
+    // FP32 (HLLC only: the LLF faces run on packed pairs, face_point_pk).  Exact-difference
+    // side quantities: r = rho, vn / vt = normal / transverse velocity, dp = pressure
+    // perturbation, H = E + p of the full state, f = flux difference
+    static_assert(HLLC, "FP32 LLF faces use face_point_pk");
+    R fL[NV], fR[NV], rs[2], vns[2], vts[2], dps[2], Hs[2], cs[2];
     R hp = A.hgam * pe;
 #pragma unroll
     for (int s = 0; s < 2; ++s) {
@@ -296,10 +278,8 @@ __device__ __forceinline__ void face_point(const StageArgs<R> &A, const R *dL, c
       dps[s] = dp;
       Hs[s] = H;
       cs[s] = c;
-      R lam = A.llf_speed == 1 ? vn + c : fabs(vn) + c;
-      if (s == 0) lamL = lam; else lamR = lam;
     }
-    if constexpr (HLLC) {
+    {
       const R SL = fmin(vns[0], vns[1]) - fmax(cs[0], cs[1]);
       const R SR = fmax(vns[0], vns[1]) + fmax(cs[0], cs[1]);
       const R DL = rs[0] * (vns[0] - SL), DR = rs[1] * (SR - vns[1]);
@@ -321,10 +301,6 @@ __device__ __forceinline__ void face_point(const StageArgs<R> &A, const R *dL, c
         F[T] = f[T] + q * (r * vts[k]);
         F[3] = f[3] + q * (Hs[k] + r * Ss * (SK - vK));
       }
-    } else {
-      R lam = A.llf_speed == 1 ? rfmax(fabs(lamR), fabs(lamL)) : rfmax(lamL, lamR);
-#pragma unroll
-      for (int v = 0; v < NV; ++v) F[v] = R(0.5) * (fR[v] + fL[v]) + R(0.5) * lam * (dL[v] - dR[v]);
     }
   }
 }
@@ -836,8 +812,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
           sfx[((2 * pp) * NQ + c) * FXS + f] = r2.x;
           sfx[((2 * pp + 1) * NQ + c) * FXS + f] = r2.y;
         }
-      continue;
-    }
+    } else {  // FP64, and the FP32 HLLC variant
     R cl[NV][NQ], cr[NV][NQ];
 #pragma unroll
     for (int v = 0; v < NV; ++v)
@@ -885,6 +860,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
     for (int v = 0; v < NV; ++v)
 #pragma unroll
       for (int b = 0; b < NQ; ++b) sfx[(v * NQ + b) * FXS + f] = mom[v][b] * A.hidx;
+    }
     } else {
     const int f = fa - FXP;
     int fi = f % TX, fj = f / TX;
@@ -942,8 +918,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
           sfy[((2 * pp) * NQ + c) * FYS + f] = r2.x;
           sfy[((2 * pp + 1) * NQ + c) * FYS + f] = r2.y;
         }
-      continue;
-    }
+    } else {  // FP64, and the FP32 HLLC variant
     R cb[NV][NQ], ct[NV][NQ];
 #pragma unroll
     for (int v = 0; v < NV; ++v)
@@ -988,6 +963,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
     for (int v = 0; v < NV; ++v)
 #pragma unroll
       for (int a = 0; a < NQ; ++a) sfy[(v * NQ + a) * FYS + f] = mom[v][a] * A.hidy;
+    }
     }
   }
   __syncthreads();
@@ -1055,7 +1031,10 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
             rbar += re * ww;
             pbar += pe * ww;
           }
-          // vol_point's exact differences, (x, y) side by side
+          // split fluxes by exact differences about a static equilibrium (u_eq velocity 0),
+          // x and y side by side:  d(rho u) = m_x,  d(rho u^2 + p) = m_x^2 / rho + dp,
+          // d(rho u v) = m_x m_y / rho,  d(u (E + p)) = u (H_eq + dE + dp),
+          // dp = (gamma - 1)(dE - |m|^2 / (2 rho))
           const float r = rfmax(re + dre.x, 1.0e-9f);
           const float inv = frcp(r);
           const float2 vel = __fmul2_rn(dm, make_float2(inv, inv));
