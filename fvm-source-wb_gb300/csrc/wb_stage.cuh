@@ -975,14 +975,73 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
   // wave-speed maxima in the kernel's precision (a maximum of floats is exact; FP64
   // arithmetic is slow on this part), widened to double only for the atomics
   R spx = R(0), spy = R(0);
+  const R *uc = su + (ty + 1) * RX + (tx + 1);  // mode m of var v at uc[(v*NB+m)*RXY]
+  R acc[NV][NB];
+#pragma unroll
+  for (int v = 0; v < NV; ++v)
+#pragma unroll
+    for (int m = 0; m < NB; ++m) acc[v][m] = R(0);
+  R rbar = R(0), pbar = R(0);
+  // The first RK input of the first output (U^n of SSP-RK2's second stage) is staged into
+  // the face-flux area once the edge integrals have read it, so its loads land during the
+  // volume quadrature instead of stalling the RK combination.  FP32, where the tile's
+  // modes fit the flux area (not the tensor P2 basis).
+  constexpr bool UN = !FP64 && NV * NB * TX * TY <= NV * NQ * (TY * (TX + 1) + (TY + 1) * TX);
+  const bool un = UN && A.o[0].out != nullptr && A.o[0].in[0] != nullptr;
+  R *sun = flux;  // [NV*NB][TX*TY]
+  auto source_edges = [&]() {
+    if constexpr (!FP64) {
+      // FP32 form: the gravity source (0, -gx drho, -gy drho, -(gx m_x + gy m_y)) is linear
+      // in the perturbation, so its Gauss projection is exactly -g times the modes
+#pragma unroll
+      for (int m = 0; m < NB; ++m) {
+        const R r = uc[(0 * NB + m) * RXY], mx = uc[(1 * NB + m) * RXY];
+        const R my = uc[(2 * NB + m) * RXY];
+        acc[1][m] -= A.gx * r;
+        acc[2][m] -= A.gy * r;
+        acc[3][m] -= A.gx * mx + A.gy * my;
+      }
+    }
+    // edge integrals: the faces' moments (already weighted by 0.5/dx, 0.5/dy)
+    const int fl = ty * (TX + 1) + tx, fb = ty * TX + tx;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      R FR[NQ], FL[NQ], GT[NQ], GB[NQ];
+#pragma unroll
+      for (int b = 0; b < NQ; ++b) {
+        FR[b] = sfx[(v * NQ + b) * FXS + fl + 1];
+        FL[b] = sfx[(v * NQ + b) * FXS + fl];
+        GT[b] = sfy[(v * NQ + b) * FYS + fb + TX];
+        GB[b] = sfy[(v * NQ + b) * FYS + fb];
+      }
+#pragma unroll
+      for (int m = 0; m < NB; ++m) {
+        int a = mode_deg(K, BASIS, m, 0), b = mode_deg(K, BASIS, m, 1);
+        acc[v][m] -= (T::Ep(a) * FR[b] - T::Em(a) * FL[b]) + (T::Ep(b) * GT[a] - T::Em(b) * GB[a]);
+      }
+    }
+
+  };
+  if (un) {
+    if (active) source_edges();
+    __syncthreads();  // every thread is done with the face fluxes
+    const R *in0 = A.o[0].in[0];
+    if (i0 + TX <= nx && j0 + TY <= ny && (nx % 4) == 0) {
+      constexpr int CPR_U = TX / 4, NCH = NV * NB * TY * CPR_U;
+      for (int k = tid; k < NCH; k += nthr) {
+        const int row = k / CPR_U, ch = k - row * CPR_U;
+        const int pl = row / TY, r = row - pl * TY;
+        cp_async<16>(sun + pl * nthr + r * TX + ch * 4,
+                     in0 + pl * P + (long long)(j0 + r) * nx + i0 + ch * 4);
+      }
+    } else if (active) {
+      const long long c0 = (long long)gj * nx + gi;
+#pragma unroll
+      for (int pl = 0; pl < NV * NB; ++pl) cp_async<sizeof(R)>(sun + pl * nthr + tid, in0 + pl * P + c0);
+    }
+    cp_async_commit();
+  }
   if (active) {
-    const R *uc = su + (ty + 1) * RX + (tx + 1);  // mode m of var v at uc[(v*NB+m)*RXY]
-    R acc[NV][NB];
-#pragma unroll
-    for (int v = 0; v < NV; ++v)
-#pragma unroll
-      for (int m = 0; m < NB; ++m) acc[v][m] = R(0);
-    R rbar = R(0), pbar = R(0);
     // the qa loops stay rolled: a third of the code for the volume quadrature, which
     // measured faster (fewer instruction-fetch stalls) than full unrolling
     if constexpr (!FP64) {
@@ -1140,37 +1199,13 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
         }
     }
     }
-    if constexpr (!FP64) {
-      // FP32 form: the gravity source (0, -gx drho, -gy drho, -(gx m_x + gy m_y)) is linear
-      // in the perturbation, so its Gauss projection is exactly -g times the modes
-#pragma unroll
-      for (int m = 0; m < NB; ++m) {
-        const R r = uc[(0 * NB + m) * RXY], mx = uc[(1 * NB + m) * RXY];
-        const R my = uc[(2 * NB + m) * RXY];
-        acc[1][m] -= A.gx * r;
-        acc[2][m] -= A.gy * r;
-        acc[3][m] -= A.gx * mx + A.gy * my;
-      }
-    }
-    // edge integrals: the faces' moments (already weighted by 0.5/dx, 0.5/dy)
-    const int fl = ty * (TX + 1) + tx, fb = ty * TX + tx;
-#pragma unroll
-    for (int v = 0; v < NV; ++v) {
-      R FR[NQ], FL[NQ], GT[NQ], GB[NQ];
-#pragma unroll
-      for (int b = 0; b < NQ; ++b) {
-        FR[b] = sfx[(v * NQ + b) * FXS + fl + 1];
-        FL[b] = sfx[(v * NQ + b) * FXS + fl];
-        GT[b] = sfy[(v * NQ + b) * FYS + fb + TX];
-        GB[b] = sfy[(v * NQ + b) * FYS + fb];
-      }
-#pragma unroll
-      for (int m = 0; m < NB; ++m) {
-        int a = mode_deg(K, BASIS, m, 0), b = mode_deg(K, BASIS, m, 1);
-        acc[v][m] -= (T::Ep(a) * FR[b] - T::Em(a) * FL[b]) + (T::Ep(b) * GT[a] - T::Em(b) * GB[a]);
-      }
-    }
-
+    if (!un) source_edges();
+  }
+  if (un) {
+    cp_async_wait<0>();
+    __syncthreads();
+  }
+  if (active) {
     // RK stage combination: out = sum c_i [lim](in_i) + beta Y + (cdt dt) L(Y).  The RK
     // inputs are read once and the outputs not re-read by this launch: streaming (.cs)
     // loads and stores keep them from displacing the staged halos in L1/L2.
@@ -1190,10 +1225,17 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
         if (o.in[ii] == nullptr) continue;
         const R *in = o.in[ii];
         R w[NV][NB];
+        if (un && oi == 0 && ii == 0) {
+#pragma unroll
+          for (int v = 0; v < NV; ++v)
+#pragma unroll
+            for (int m = 0; m < NB; ++m) w[v][m] = sun[(v * NB + m) * nthr + tid];
+        } else {
 #pragma unroll
         for (int v = 0; v < NV; ++v)
 #pragma unroll
           for (int m = 0; m < NB; ++m) w[v][m] = __ldcs(in + (long long)(v * NB + m) * P + cell);
+        }
         if (POS && o.lim[ii] && A.limiter == 2 && K >= 1) {
           R dl[NV * NB];
 #pragma unroll
