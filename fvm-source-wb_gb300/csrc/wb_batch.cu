@@ -1,6 +1,8 @@
 // wb_batch.cu -- batched form: n independent instances (own grid, degree, equilibrium,
-// perturbation) advanced together by one persistent launch per RK stage over a work
-// list of cell tiles, with the step sequence replayed from a CUDA graph.
+// perturbation) advanced together, per RK stage one persistent launch per group (the
+// instances of one degree on one tile shape) over the group's work list of cell tiles,
+// with the step sequence replayed from a CUDA graph.  wb_batch_autotune picks each
+// (degree, size class) group's tile by timing.
 //
 // Each instance is a full FP32-perturbation context (its own state buffers, equilibrium
 // tables and run state, hence its own CFL time step); the batch owns the work list, the
