@@ -1042,13 +1042,13 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
     cp_async_commit();
   }
   if (active) {
-    // the qa loops stay rolled: a third of the code for the volume quadrature, which
-    // measured faster (fewer instruction-fetch stalls) than full unrolling
+    // The FP64 qa loop stays rolled (a third of the code, fewer instruction-fetch stalls);
+    // the packed FP32 loop is short enough to unroll, which measured 1 % faster.
     if constexpr (!FP64) {
       // FP32 on packed pairs: point values as (rho, E) and (m_x, m_y), split fluxes as
       // (Fx, Fy) of one variable, projections as (P_b, Q_{b+1}) with P_b = sum Fx BW(b),
       // Q_b = sum Fy DW(b) (the 0.5/dy goes into bwy below)
-#pragma unroll 1
+#pragma unroll
       for (int qa = 0; qa < NQ; ++qa) {
         float2 cre[NQ], cmm[NQ];
 #pragma unroll
