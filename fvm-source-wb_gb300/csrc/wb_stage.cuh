@@ -7,10 +7,14 @@
 //      Zhang-Shu positivity limiter (limit-on-load: stage outputs are stored unlimited
 //      and every consumer limits what it reads, which is the same as the reference's
 //      apply_limiter after each stage);
-//   3. computes every x- and y-face flux of the tile once (LLF on equilibrium face
-//      state + perturbation traces, minus the equilibrium flux);
+//   3. computes every x- and y-face flux of the tile once (LLF or HLLC on equilibrium
+//      face state + perturbation traces, minus the equilibrium flux);
 //   4. per cell: volume and source quadrature of the split fluxes, edge integrals,
 //      assembly, the RK stage combination, and (last stage) the CFL wave-speed maxima.
+//      In FP32 the edge integrals come first; the face-flux area then receives the
+//      tile's first RK input by cp.async while the volume quadrature runs.
+// Interior tiles of the persistent kernel are staged by one TMA copy, the rest by
+// cp.async; the next tile is staged while the current one is computed.
 // The reference computes the same quantities in separate whole-array passes
 // (2d/benchmark_2d_dg.f90:1137-1479 for the operator, :666-747 for the stage loop,
 // :826-870 for the wave speed).
