@@ -323,9 +323,18 @@ int wb_batch_autotune(wb_batch *b, int32_t reps, int32_t *tiles) {
   // which that launch rewrites too, so the instances' states are not changed.
   const StageArgs<float> *a1 = b->args + ((size_t)b->phase * 2 + 0) * n;
   static const int cand[2][2] = {{32, 8}, {16, 16}};
+  // The candidates' items go through the work-list buffer, which a captured graph reads
+  // (and which may be reallocated): the graph goes first.
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   BCK(cudaEventCreate(&e0));
-  BCK(cudaEventCreate(&e1));
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return berr(b, WB_ERR_CUDA, "cudaEventCreate failed");
+  }
   rc = WB_OK;
   for (int K = 0; K < 3 && !rc; ++K)
     for (int cls = 0; cls < 2 && !rc; ++cls) {
@@ -362,8 +371,10 @@ int wb_batch_autotune(wb_batch *b, int32_t reps, int32_t *tiles) {
     }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  // the real work list again, also after a failure (the buffer holds candidate items)
+  const int rw = build_worklist(b);
   if (rc) return rc;
-  if ((rc = build_worklist(b))) return rc;
+  if (rw) return rw;
   if (tiles)
     for (int K = 0; K < 3; ++K)
       for (int cls = 0; cls < 2; ++cls) {
