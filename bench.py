@@ -159,9 +159,9 @@ def cpu_sample(wb, seconds=12.0, n=512, min_steps=2, warm=1, threads=None):
         d, _ = O.run_rk2(oc, d, 1, -1.0)
         steps += 1
     el = time.perf_counter() - t0
-    desc = ("FP64 oracle port (C, OpenMP) on %dx%d cells of the cfg5 physics (P2, "
-            "isothermal Phi=0.1y, 16-mode velocity field), %d SSP-RK2 CFL steps, %.1f s"
-            % (n, n, steps, el))
+    desc = ("FP64 oracle port (C, OpenMP, %d thread%s) on %dx%d cells of the cfg5 physics "
+            "(P2, isothermal Phi=0.1y, 16-mode velocity field), %d SSP-RK2 CFL steps, %.1f s"
+            % (threads, "" if threads == 1 else "s", n, n, steps, el))
     return dof * steps / el, threads, desc
 
 
@@ -239,6 +239,71 @@ def batch_leg(wb, n, dev, steps=24, warmup=6):
             "workload": "%d instances: N = exp(U(ln 32, ln 512)), degree 0..2 (P basis), "
                         "isothermal or polytrope, Gaussian bump 10^U(-6,-2); FP32, SSP-RK2, "
                         "CFL steps" % len(cfgs)}
+
+
+def batch_accuracy(wb, n, dev, steps=20):
+    """The batched form's FP32 instances against FP64 plain contexts of the same instances
+    (same seeded workload), after `steps` fixed steps of one dt that satisfies every
+    instance's CFL condition: L1 / Linf per conserved variable of the difference, maximum
+    over the instances (norms in FP64 on the device, wb_norms)."""
+    cfgs, ics = wb.batch_workload(n=n, device=dev)
+    # one dt for all: the smallest instance CFL step (FP64 wave speeds of the initial state)
+    dts = []
+    for c, ic in zip(cfgs, ics):
+        c64 = wb.default_config(**{k: getattr(c, k) for k, _ in wb.WbConfig._fields_})
+        c64.precision = wb.PREC_FP64
+        with wb.Solver(config=c64) as s:
+            s.init_perturbation(ic)
+            sx, sy = s.compute_max_speed()
+            dts.append(c.cfl / (2 * c.order + 1) / (sx * c.nx / c.lx + sy * c.ny / c.ly))
+    dt = 0.9 * min(dts)
+    t0 = time.perf_counter()
+    with wb.Batch(cfgs) as bt:
+        bt.init_perturbation(ics)
+        bt.step(steps, dt)
+        bt.sync()
+        worst_l1, worst_linf, worst_rel = np.zeros(4), np.zeros(4), 0.0
+        for i, (c, ic) in enumerate(zip(cfgs, ics)):
+            c64 = wb.default_config(**{k: getattr(c, k) for k, _ in wb.WbConfig._fields_})
+            c64.precision = wb.PREC_FP64
+            with wb.Solver(config=c64) as ref, wb.Solver(config=c64) as got:
+                ref.init_perturbation(ic)
+                ref.step(steps, dt)
+                got.upload(bt.download(i))
+                l1, linf, _ = got.compute_error(ref)
+                p1, _, _ = ref.compute_error(None)
+            worst_l1 = np.maximum(worst_l1, l1)
+            worst_linf = np.maximum(worst_linf, linf)
+            worst_rel = max(worst_rel, float(np.max(l1 / np.maximum(p1, 1e-300))))
+    return {"instances": len(cfgs), "steps": steps, "dt": dt,
+            "l1_fp32_vs_fp64_max": worst_l1.tolist(), "linf_fp32_vs_fp64_max": worst_linf.tolist(),
+            "l1_relative_to_perturbation_max": worst_rel, "l1_bar": 1e-6,
+            "pass": bool(np.all(worst_l1 <= 1e-6)), "seconds": time.perf_counter() - t0,
+            "reference": "FP64 plain context of each instance, same dt and steps"}
+
+
+def limited_leg(wb, name, dev, steps=6, warmup=3):
+    """The headline grid with the minmod limiter on the perturbation (limit-on-load inside
+    the stage kernel: the means halo is staged too): DOF-updates/s by CUDA events."""
+    import torch
+    w = wb.workload(name, wb.PREC_FP32, limiter=1, device=dev)
+    with wb.Solver(**w) as s:
+        s.init_perturbation(wb.workload_ic(name))
+        s.step(warmup)
+        s.sync()
+        st = torch.cuda.ExternalStream(s.stream(), device=dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        s.step(steps)
+        e1.record(st)
+        e1.synchronize()
+        s.sync()
+        ms = e0.elapsed_time(e1)
+        dof = s.dofs
+    return {"value": dof * steps / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / steps,
+            "steps": steps, "limiter": "minmod (compute_limiter on the perturbation)",
+            "workload": "%s with the minmod limiter" % name}
 
 
 def run_batch_only(args):
@@ -381,15 +446,24 @@ def run_ours(args):
                             "path": "wb_upload_state_f32 + wb_step + wb_download_state_f32"}}
     s32.close()
 
-    # the batched form (512 independent instances, one persistent launch per stage, CUDA
-    # graph of six steps): reported beside the headline, not part of it
+    # beside the headline, not part of it: the grid with the minmod limiter on; the
+    # batched form (512 independent instances, CUDA graph of six steps) and its accuracy
+    # against FP64 instances; the cfg3 accuracy study (FP32 form vs FP64 plain, 500 steps)
     if rank == 0 and not args.quick:
+        extra["limited"] = limited_leg(wb, name, dev)
         extra["batch"] = batch_leg(wb, 512, dev)
+        extra["batch"]["accuracy"] = batch_accuracy(wb, 512, dev)
+        if args.accuracy_steps > 0:
+            extra["accuracy_cfg3"] = accuracy_cfg3(wb, args.accuracy_steps, dev)
 
     cpu = None
     if rank == 0 and not args.quick:
         v, cores, desc = cpu_sample(wb, seconds=args.cpu_seconds)
         cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc}
+        # the reference is serial: the same port on one core, on a smaller sample
+        v1, _, desc1 = cpu_sample(wb, seconds=args.cpu_seconds, n=128, threads=1)
+        cpu["one_core"] = {"value": v1, "unit": UNIT, "cores": 1, "kind": "port",
+                           "sample": desc1}
 
     if rank == 0:
         line = {
@@ -413,21 +487,16 @@ def run_ours(args):
     return 0
 
 
-def run_accuracy(args):
+def accuracy_cfg3(wb, n, dev=0):
     """The accuracy configuration (cfg3): 2048^2 P2 polytrope K = 1, Phi = y, seeded Gaussian
     pressure bump (sigma 0.05) of amplitude 1e-1, 1e-3 and 1e-6; the FP32 perturbation form
-    against the FP64 plain method over the same fixed time steps (dt from the initial CFL
-    speed of the FP64 run).  Prints one JSON line: L1 / Linf per conserved variable of the
-    difference (unit-area domain, so L1 is a mean absolute error) and of the perturbation."""
-    import torch
-    wb = load_package()
-    wb.lib()
-    torch.cuda.set_device(0)
-    n = args.accuracy_steps
+    against the FP64 plain method over the same n fixed time steps (dt from the initial CFL
+    speed of the FP64 run): L1 / Linf per conserved variable of the difference (unit-area
+    domain, so L1 is a mean absolute error) and of the perturbation."""
     results = []
     for amp in (1e-1, 1e-3, 1e-6):
-        w64 = wb.workload("cfg3", wb.PREC_FP64)
-        w32 = wb.workload("cfg3", wb.PREC_FP32)
+        w64 = wb.workload("cfg3", wb.PREC_FP64, device=dev)
+        w32 = wb.workload("cfg3", wb.PREC_FP32, device=dev)
         ic = wb.workload_ic("cfg3", amp)
         with wb.Solver(**w64) as s64, wb.Solver(**w32) as s32:
             s64.init_perturbation(ic)
@@ -447,10 +516,21 @@ def run_accuracy(args):
                         "linf_fp32_vs_fp64": linf.tolist(), "l1_perturbation": p1.tolist(),
                         "linf_perturbation": pinf.tolist(), "dt": dt, "seconds": el,
                         "pass": bool(np.all(l1 <= 1e-6))})
-    print(json.dumps({"mode": "accuracy",
-                      "workload": "cfg3: 2048^2 P2 polytrope K=1, Phi=y, Gaussian pressure bump "
-                                  "(sigma 0.05, seed 3), FP32 perturbation vs FP64 plain",
-                      "steps": n, "l1_bar": 1e-6, "results": results}))
+    return {"workload": "cfg3: 2048^2 P2 polytrope K=1, Phi=y, Gaussian pressure bump "
+                        "(sigma 0.05, seed 3), FP32 perturbation vs FP64 plain, fixed dt",
+            "steps": n, "l1_bar": 1e-6, "pass": all(r["pass"] for r in results),
+            "results": results}
+
+
+def run_accuracy(args):
+    """The cfg3 accuracy study alone (one JSON line)."""
+    import torch
+    wb = load_package()
+    wb.lib()
+    torch.cuda.set_device(0)
+    line = {"mode": "accuracy"}
+    line.update(accuracy_cfg3(wb, args.accuracy_steps))
+    print(json.dumps(line))
     return 0
 
 

@@ -99,6 +99,10 @@ def lib():
             "wb1d_last_error": ([p], ctypes.c_char_p), "wb1d_upload": ([p, p], i32),
             "wb1d_download": ([p, p], i32), "wb1d_compute_update": ([p, p, p], i32),
             "wb1d_evolve": ([p, d, i32, p, p], i32),
+            "wb1d_write_dat": ([p, ctypes.c_char_p, i32], i32),
+            "wb_read_dat": ([ctypes.c_char_p, i32, p, ctypes.c_int64, p], i32),
+            "wb_norms_device_noalloc": ([i32, i32, i32, i32, d, d, p, p, ctypes.c_size_t, p,
+                                         p, p, p], i32),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -122,6 +126,28 @@ def mode_list(order, basis):
     b = np.zeros(n, np.int32)
     lib().wb_mode_list(order, basis, _ptr(a), _ptr(b))
     return a, b
+
+
+def read_dat(path, ncols):
+    """Records of a text snapshot in the reference's '(7(1PE12.5,1X))' format as an
+    (nrows, ncols) array (wb_read_dat; a host-only call, no GPU needed)."""
+    cap = os.path.getsize(path) // (13 * ncols) + 1  # every value takes 13 columns
+    out = np.zeros((cap, ncols))
+    n = ctypes.c_int64()
+    rc = lib().wb_read_dat(os.fsencode(path), int(ncols), _ptr(out), cap, ctypes.byref(n))
+    if rc != WB_OK:
+        raise WbError(rc, "cannot read %s as %d-column records" % (path, ncols))
+    return out[:n.value].copy()
+
+
+def read_output_file(path, nx, ny, var=1):
+    """A 2D snapshot of output_file read back as get_image does (post_processing2d.py:55-64):
+    x, y and the fields w - w_eq of variables var..4, each shaped (nx, ny)."""
+    data = read_dat(path, 2 + 5 - var)
+    if data.shape[0] != nx * ny:
+        raise WbError(WB_ERR_ARG, "%s holds %d records, not %d" % (path, data.shape[0], nx * ny))
+    cols = [data[:, k].reshape(nx, ny) for k in range(data.shape[1])]
+    return cols[0], cols[1], cols[2:]
 
 
 def default_config(**kw):
@@ -642,3 +668,14 @@ class Solver1D:
         self._check(lib().wb1d_evolve(self._c, float(tend), int(max_steps), ctypes.byref(n),
                                       ctypes.byref(t)))
         return n.value, t.value
+
+    def output_file(self, path, var=3):
+        """Text snapshot in benchmark_1d.f90's output_file format: x and w - w_eq of the
+        primitive variables var..3 at the cell centres (the reference writes var = 3)."""
+        self._check(lib().wb1d_write_dat(self._c, os.fsencode(path), int(var)))
+
+    @staticmethod
+    def read_output_file(path, var=3):
+        """(x, [w - w_eq for variables var..3]) of a 1D snapshot."""
+        data = read_dat(path, 1 + 4 - var)
+        return data[:, 0], [data[:, k] for k in range(1, data.shape[1])]

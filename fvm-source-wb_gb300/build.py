@@ -16,7 +16,7 @@ NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 SOURCES = ["wb_kernels_f64.cu", "wb_kernels_f32.cu", "wb_capi.cu", "wb_batch.cu", "wb_fv1d.cu",
-           "wb_noalloc.cu", "wb_stage_dispatch.cu", "wb_tables.cpp"]
+           "wb_noalloc.cu", "wb_stage_dispatch.cu", "wb_tables.cpp", "wb_dat.cpp"]
 GEN = os.path.join(OUT, "gen")
 
 

@@ -1123,19 +1123,6 @@ int wb_get_time(wb_ctx *ctx, double *t, int64_t *steps) {
   return WB_OK;
 }
 
-// Fortran 1PE12.5: one digit before the point, five after, exponent E+dd (or +ddd with
-// the E dropped when the exponent needs three digits), right-justified in 12 columns.
-static void fortran_1pe12_5(double v, char *out) {
-  char buf[64];
-  std::snprintf(buf, sizeof(buf), "%.5E", v);
-  char *e = std::strchr(buf, 'E');
-  if (e) {
-    int ex = std::atoi(e + 1);
-    if (ex >= 100 || ex <= -100) std::snprintf(e, 8, "%c%03d", ex < 0 ? '-' : '+', ex < 0 ? -ex : ex);
-  }
-  std::snprintf(out, 16, "%12s", buf);
-}
-
 int wb_write_dat(wb_ctx *ctx, const char *path, int32_t var) {
   if (!ctx || !path || var < 1 || var > 4) return WB_ERR_ARG;
   const wb_config &g = ctx->cfg;

@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -371,6 +372,39 @@ int wb1d_evolve(wb1d_ctx *c, double tend, int32_t max_steps, int32_t *steps_done
   if (steps_done) *steps_done = n;
   if (t_out) *t_out = t;
   if (!std::isfinite(t)) return e1(c, WB_ERR_NONPHYSICAL, "non-finite time step");
+  return WB_OK;
+}
+
+int wb1d_write_dat(wb1d_ctx *c, const char *path, int32_t var) {
+  if (!c || !path || var < 1 || var > 3) return WB_ERR_ARG;
+  const int nx = c->cfg.nx;
+  std::vector<double> d((size_t)3 * nx);
+  int rc = wb1d_download(c, d.data());
+  if (rc) return rc;
+  wb::EqParams ep{c->cfg.eq_kind, c->cfg.gamma, c->cfg.g, 0.0, c->cfg.rho0, c->cfg.p0, c->cfg.kpoly};
+  const double dx = c->cfg.lx / (double)nx, gm1 = c->cfg.gamma - 1.0, fy = wb::eq_factor_y(ep, 0.0);
+  FILE *f = std::fopen(path, "w");
+  if (!f) return e1(c, WB_ERR_ARG, std::string("cannot open ") + path);
+  char num[16];
+  for (int i = 0; i < nx; ++i) {
+    // primitive state of the full cell value u_eq + delta minus the equilibrium's
+    // primitives at the centre: (rho - rho_eq, u, p - p_eq)
+    const double x = ((double)i + 0.5) * dx;
+    double re, pe;
+    wb::eq_combine(ep, wb::eq_factor_x(ep, x), fy, &re, &pe);
+    const double *u = &d[(size_t)i * 3];
+    const double rho = re + u[0], v = u[1] / rho;
+    const double p = gm1 * (pe / gm1 + u[2] - 0.5 * rho * v * v);
+    const double w[3] = {rho - re, v, p - pe};
+    wb::fortran_1pe12_5(x, num);
+    std::fprintf(f, "%s ", num);
+    for (int k = var - 1; k < 3; ++k) {
+      wb::fortran_1pe12_5(w[k], num);
+      std::fprintf(f, "%s ", num);
+    }
+    std::fprintf(f, "\n");
+  }
+  std::fclose(f);
   return WB_OK;
 }
 

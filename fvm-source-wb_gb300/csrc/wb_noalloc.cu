@@ -6,8 +6,10 @@
 // that must not pay the device-wide synchronisation cudaMalloc/cudaFree imply.  For them
 // this entry point keeps its reduction scratch in a fixed array that is part of the
 // library image: it exists on every device that loads the library, for the life of the
-// process.  The first call on a device sets the device up; calls sharing the array must
+// process.  The first call on a device (and again after the device's context has been
+// re-created, e.g. by cudaDeviceReset) sets the device up; calls sharing the array must
 // not overlap on the GPU.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -45,6 +47,7 @@ static __device__ __align__(256) wb::Tab1D<double> g_norm_tabs[wb::KMAX + 1];
 
 struct DeviceSetup {
   bool done = false;
+  unsigned long long ctx_id = 0;       // the CUDA context the set-up was done in
   double *scratch = nullptr;           // device address of g_norm_scratch
   wb::Tab1D<double> *tabs = nullptr;   // device address of g_norm_tabs
 };
@@ -52,11 +55,43 @@ constexpr int kMaxDevices = 64;
 DeviceSetup g_setup[kMaxDevices];
 std::mutex g_setup_mutex;
 
-// Once per device, with that device current: the symbol addresses (a host-side name of
-// a __device__ array is not a device address) and the basis tables.
+// Unique id of the current CUDA context (cuCtxGetId through the runtime's driver entry
+// point, no link to libcuda), 0 where it is not available.  A context torn down by
+// cudaDeviceReset and created again gets a new id, and with it new copies of the arrays.
+unsigned long long current_context_id() {
+  using GetCurrent = CUresult (*)(CUcontext *);
+  using GetId = CUresult (*)(CUcontext, unsigned long long *);
+  static std::once_flag once;
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrent>(p);
+    p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetId>(p);
+    cudaGetLastError();
+  });
+  CUcontext c = nullptr;
+  unsigned long long id = 0;
+  if (get_current && get_id && get_current(&c) == CUDA_SUCCESS && c && get_id(c, &id) == CUDA_SUCCESS)
+    return id;
+  return 0;
+}
+
+// Once per device and context, with that device current (the runtime has made its
+// primary context current): the symbol addresses (a host-side name of a __device__ array
+// is not a device address) and the basis tables.
 int setup_device(int dev, DeviceSetup **out) {
   std::lock_guard<std::mutex> lock(g_setup_mutex);
   DeviceSetup &s = g_setup[dev];
+  // no context current yet (id 0) or another one than at set-up: set up (again); the
+  // runtime calls below make the device's context current
+  if (s.done && (s.ctx_id == 0 || s.ctx_id != current_context_id())) s = DeviceSetup();
   if (!s.done) {
     void *p = nullptr;
     if (cudaGetSymbolAddress(&p, g_norm_scratch) != cudaSuccess) return WB_ERR_CUDA;
@@ -66,6 +101,7 @@ int setup_device(int dev, DeviceSetup **out) {
     wb::Tab1D<double> t[wb::KMAX + 1];
     wb::make_tab1d(t);
     if (cudaMemcpyToSymbol(g_norm_tabs, t, sizeof(t)) != cudaSuccess) return WB_ERR_CUDA;
+    s.ctx_id = current_context_id();
     s.done = true;
   }
   *out = &s;

@@ -31,4 +31,9 @@ void make_eq_tables(const EqParams &e, int nx, int ny, double lx, double ly, int
                     const double *xq, std::vector<double> &fxv, std::vector<double> &fxf,
                     std::vector<double> &fyv, std::vector<double> &fyf);
 
+// The reference's snapshot number format, Fortran 1PE12.5 (12 columns, E+dd, or +ddd with
+// the E dropped for three-digit exponents), into out[16]; and its reader.
+void fortran_1pe12_5(double v, char *out);
+bool parse_fortran_real(const char *tok, double *v);
+
 }  // namespace wb

@@ -4,7 +4,7 @@
  * Drop-in boundary for the step routines of hanveiga/fvm-source-wb.  The reference
  * binds them as Fortran external subroutines with implicit interfaces and sizes taken
  * from module parameters; a Fortran driver reaches this library through an
- * ISO_C_BINDING interface module (bind(C, name="wb_...")), see INTEGRATION.md.
+ * ISO_C_BINDING interface module (bind(C, name="wb_...")) declared against this header.
  *
  * Conventions
  *   - every entry point returns an int status: WB_OK (0) or a negative WB_ERR_* code;
@@ -203,16 +203,20 @@ int wb_norms(wb_ctx *ctx, wb_ctx *other, double l1[4], double linf[4], double l2
 int wb_conserved_sums(wb_ctx *ctx, double sums[4]);
 
 /* Error norms (L1, Linf, L2 per conserved variable, as wb_norms) of two device-resident
- * FP64 modal states a and b (SoA, plane_stride elements between (variable, mode) planes;
- * b may be NULL for the norms of a) that allocates no device memory.  No counterpart in
+ * FP64 modal states a and b (SoA, plane_stride elements between (variable, mode) planes,
+ * the same stride and [variable][mode][plane] layout for both -- wb_device_state gives a
+ * context's; b may be NULL for the norms of a) that allocates no device memory.  No counterpart in
  * the reference.  It is for callers that cannot call cudaMalloc where they need the norms:
  * a host whose device memory is all owned by its own pool or by another runtime, or a time
  * loop that must not take the device-wide synchronisation cudaMalloc/cudaFree imply.
  * Its reduction scratch is a fixed array inside the library, 1.5 MB on every device that
  * loads the library and held until the process exits, so grids are limited to
- * WB_NORMS_NOALLOC_MAX_CELLS cells; a larger grid returns WB_ERR_ARG (use wb_norms).  The
- * first call on a device sets that device up (looks up the array's device address and
- * uploads the basis tables): make the first call before any stream capture.  Every call
+ * WB_NORMS_NOALLOC_MAX_CELLS cells, and a grid whose 32x8-cell blocks outnumber the
+ * array's 16,384 partial slots (a narrow grid such as 33 x 127,000) returns WB_ERR_ARG too
+ * (use wb_norms).  The first call on a device sets that device up (looks up the array's
+ * device address and uploads the basis tables): make the first call before any stream
+ * capture.  The set-up belongs to the device's CUDA context: after that context is torn
+ * down (cudaDeviceReset) and created again, the next call sets the device up again.  Every call
  * uses the same array, so calls that overlap on the GPU (other streams, other threads)
  * race.  stream may be NULL (the default stream); the call waits for it before it returns
  * the host results. */
@@ -225,6 +229,14 @@ int wb_norms_device_noalloc(int32_t nx, int32_t ny, int32_t order, int32_t basis
  * and the primitive perturbation w - w_eq there for variables var..4, each written as
  * Fortran 1PE12.5 followed by one blank. */
 int wb_write_dat(wb_ctx *ctx, const char *path, int32_t var);
+/* Reads a text snapshot written in that format ('(7(1PE12.5,1X))', one record per line,
+ * a record of more than 7 values continued on the next lines, 7 per line) into
+ * values[row * ncols + col]; *nrows receives the records read.  Accepts the E-less
+ * three-digit exponent form (1.23456-100).  WB_ERR_ARG for a missing file, a token that
+ * is not a number, a record of another length, or more than `capacity` records.  The
+ * reference reads its snapshots with np.loadtxt in get_image (post_processing2d.py:55-64):
+ * columns x, y, then the fields, reshaped to (nx, ny) with y fastest.  Host only. */
+int wb_read_dat(const char *path, int32_t ncols, double *values, int64_t capacity, int64_t *nrows);
 
 /* --- batched form -------------------------------------------------------------- */
 typedef struct wb_batch wb_batch;
@@ -270,6 +282,11 @@ int wb1d_upload(wb1d_ctx *c, const double *delta);      /* delta[i*3 + v] */
 int wb1d_download(wb1d_ctx *c, double *delta);
 int wb1d_compute_update(wb1d_ctx *c, const double *delta, double *dudt);
 int wb1d_evolve(wb1d_ctx *c, double tend, int32_t max_steps, int32_t *steps_done, double *t_out);
+/* Text snapshot of the 1D state: output_file, benchmark_1d.f90:69-100 -- one line per cell
+ * with the cell centre x and the primitive perturbation w - w_eq at the centre for
+ * variables var..3 of (rho, u, p) (the reference writes var = 3), each as 1PE12.5 and a
+ * blank; read back with wb_read_dat. */
+int wb1d_write_dat(wb1d_ctx *c, const char *path, int32_t var);
 
 #ifdef __cplusplus
 }

@@ -150,3 +150,56 @@ def test_set_equilibrium_matches_fresh_context(wb, precision):
         with pytest.raises(RuntimeError):
             a.set_equilibrium(7, 0.0, 0.0)
         assert a.cfg.eq_kind == 2   # a rejected call changes nothing
+
+
+@pytest.mark.parametrize("var", [1, 3])
+def test_output_file_round_trip_2d(wb, orc, tmp_path, var):
+    """output_file -> wb_read_dat (as get_image reads it) -> the primitive perturbation at
+    every cell's first Gauss point, to the format's six significant digits."""
+    c = base_cfg(nx=9, ny=7, order=2, basis=1, eq_kind=2, gx=0.2, gy=0.9)
+    d = random_delta(c, amp=1e-2, seed=18)
+    with solver(wb, c, 0) as s:
+        s.upload(d)
+        s.step(2, 1e-3)
+        s.output_file(str(tmp_path / "snap.dat"), var=var)
+        dl = s.download()
+    x, y, fields = wb.read_output_file(str(tmp_path / "snap.dat"), 9, 7, var=var)
+    assert x.shape == (9, 7) and len(fields) == 5 - var
+    oc = orc_cfg(c)
+    nodes = orc.nodes_from_modes(oc, dl)
+    xg, _ = orc.gl(3)
+    for i in range(9):
+        for j in range(7):
+            xq = (i + 0.5) / 9 + 0.5 / 9 * xg[0]
+            yq = (j + 0.5) / 7 + 0.5 / 7 * xg[0]
+            re, pe = orc.eq_at(oc, xq, yq)
+            u = nodes[:, 0, j, i] + np.array([re, 0, 0, pe / 0.4])
+            w = [u[0] - re, u[1] / u[0], u[2] / u[0],
+                 0.4 * (u[3] - 0.5 * (u[1] ** 2 + u[2] ** 2) / u[0]) - pe]
+            np.testing.assert_allclose([x[i, j], y[i, j]], [xq, yq], rtol=5e-6)
+            np.testing.assert_allclose([f[i, j] for f in fields], w[var - 1:], rtol=5e-6,
+                                       atol=1e-300)
+
+
+@pytest.mark.parametrize("var", [1, 3])
+def test_output_file_round_trip_1d(wb, orc, tmp_path, var):
+    """The 1D output_file (benchmark_1d.f90:69-100): x and w - w_eq at the cell centres,
+    read back through wb_read_dat, to six significant digits."""
+    c = orc.make_fv1d(nx=64, bc=1, limiter=1, eq_kind=1, cfl=0.4)
+    d0 = orc.fv1d_ic(c)
+    with wb.Solver1D(nx=64, bc=1, limiter=1, eq_kind=1, cfl=0.4) as s:
+        s.upload(d0)
+        s.evolve(0.05)
+        got = s.download()
+        s.output_file(str(tmp_path / "snap1d.dat"), var=var)
+    lines = open(tmp_path / "snap1d.dat").read().splitlines()
+    assert len(lines) == 64 and all(len(ln) == (1 + 4 - var) * 13 for ln in lines)
+    x, fields = wb.Solver1D.read_output_file(str(tmp_path / "snap1d.dat"), var=var)
+    re, pe = orc.fv1d_eq_cells(c)
+    rho = re + got[:, 0]
+    v = got[:, 1] / rho
+    p = 0.4 * (pe / 0.4 + got[:, 2] - 0.5 * rho * v * v)
+    w = [rho - re, v, p - pe]
+    np.testing.assert_allclose(x, (np.arange(64) + 0.5) / 64, rtol=5e-6)
+    for k, f in enumerate(fields):
+        np.testing.assert_allclose(f, w[var - 1 + k], rtol=5e-6, atol=1e-300)

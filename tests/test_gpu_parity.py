@@ -216,9 +216,14 @@ def test_evolve_reaches_tend(wb, orc):
         n, t = s.evolve(0.05)
         got = s.download()
     assert abs(t - 0.05) < 1e-15
-    ref, tref = orc.run_rk2(orc_cfg(c), d, n, -1.0)
-    # the oracle's last step is not clipped at tend, so compare all but the last step
     assert n > 3
+    # evolve = n - 1 CFL steps, then one step clipped at tend (dt = tend - t); the oracle
+    # runs the same sequence
+    oc = orc_cfg(c)
+    ref, tref = orc.run_rk2(oc, d, n - 1, -1.0)
+    assert tref < 0.05
+    ref, _ = orc.run_rk2(oc, ref, 1, 0.05 - tref)
+    assert np.all(rel_l1_full(c, got, ref) < 1e-12)
 
 
 @pytest.mark.parametrize("precision", [0, 1])

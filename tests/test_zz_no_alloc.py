@@ -66,3 +66,38 @@ def test_noalloc_rejects_grids_beyond_its_scratch(wb):
         rc = f(4096, 2048, 1, 1, 1.0, 1.0, pa, None, 4096 * 2048, None, _ptr(l1), _ptr(linf),
                _ptr(l2))
         assert rc == wb.WB_ERR_ARG
+
+
+def test_noalloc_at_its_largest_partial_array_on_a_stream(wb):
+    """2048 x 2048 cells fill all 16,384 partial slots of the fixed scratch; the call runs on
+    the context's own (non-default) stream, twice in a row, against wb_norms."""
+    f = _entry(wb)
+    c = base_cfg(nx=2048, ny=2048, order=1, basis=1, limiter=0, bc_x=0)
+    with solver(wb, c, 0) as a, solver(wb, c, 0) as b:
+        a.init_perturbation(wb.seeded_multimode(5, 16, 1e-2, 8))
+        b.init_perturbation(wb.seeded_gaussian_bump(3, 1e-1, 0.05))
+        r1, rinf, r2 = a.compute_error(b)
+        pa, plane = a.device_state()
+        pb, _ = b.device_state()
+        for _ in range(2):
+            l1, linf, l2 = np.zeros(4), np.zeros(4), np.zeros(4)
+            rc = f(c["nx"], c["ny"], c["order"], c["basis"], c["lx"], c["ly"], pa, pb, plane,
+                   a.stream(), _ptr(l1), _ptr(linf), _ptr(l2))
+            assert rc == wb.WB_OK
+            np.testing.assert_allclose(l1, r1, rtol=1e-13)
+            np.testing.assert_allclose(linf, rinf, rtol=1e-13)
+            np.testing.assert_allclose(l2, r2, rtol=1e-13)
+
+
+def test_noalloc_rejects_narrow_grids_with_too_many_blocks(wb):
+    """33 x 127000 cells are fewer than the cell limit but need 31,750 blocks of 32x8
+    cells, more than the scratch's 16,384 partial slots: rejected before any launch."""
+    f = _entry(wb)
+    c = base_cfg(nx=8, ny=8, order=1, basis=1)
+    assert 33 * 127000 <= 4194304
+    with solver(wb, c, 0) as a:
+        pa, _ = a.device_state()
+        l1, linf, l2 = np.zeros(4), np.zeros(4), np.zeros(4)
+        rc = f(33, 127000, 1, 1, 1.0, 1.0, pa, None, 33 * 127000, None, _ptr(l1), _ptr(linf),
+               _ptr(l2))
+        assert rc == wb.WB_ERR_ARG
