@@ -231,7 +231,7 @@ def batch_leg(wb, n, dev, steps=24, warmup=6):
     achieved = BYTES_PER_DOF_UPDATE["fp32"] * dofs * steps / el / 1e9
     return {"value": dofs * steps / el, "unit": UNIT, "instances": len(cfgs), "dofs": dofs,
             "steps": steps, "ms_per_step": el / steps * 1e3,
-            "tiles": {"K%d_%s" % (k, "small" if c == 0 else "large"): "%dx%d" % t
+            "tiles": {"K%d_%s" % (k, "small" if c == 0 else "large"): "%dx%d/%d" % t
                       for (k, c), t in sorted(tiles.items())},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
@@ -324,16 +324,17 @@ def run_ours(args):
     name = args.workload
     size = {} if args.nx <= 0 else {"nx": args.nx, "ny": args.nx}
     fixed = {}
-    if args.tile:
-        tx, ty = (int(v) for v in args.tile.lower().split("x"))
-        fixed = {"tile_x": tx, "tile_y": ty}
+    if args.tile:  # TXxTY or TXxTY/CPT
+        shape, _, cpt = args.tile.lower().partition("/")
+        tx, ty = (int(v) for v in shape.split("x"))
+        fixed = {"tile_x": tx, "tile_y": ty, "cells_per_thread": int(cpt or 1)}
     w32 = wb.workload(name, wb.PREC_FP32, **size, **fixed)
     ic = wb.workload_ic(name)
     s32 = wb.Solver(device=dev, **w32)
     dof = s32.dofs
     s32.init_perturbation(ic)
     # fastest compiled tile shape for this grid (state preserved), unless one is given
-    tile = (fixed["tile_x"], fixed["tile_y"]) if fixed else s32.autotune(2)
+    tile = (fixed["tile_x"], fixed["tile_y"], fixed["cells_per_thread"]) if fixed else s32.autotune(2)
     s32.step(args.warmup)
     s32.sync()
     stream = torch.cuda.ExternalStream(s32.stream(), device=dev)
@@ -549,7 +550,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--nx", type=int, default=0,
                     help="cells per side instead of the workload's (small cases for profiling)")
-    ap.add_argument("--tile", default="", help="fixed stage tile TXxTY (default: autotune)")
+    ap.add_argument("--tile", default="",
+                    help="fixed stage tile TXxTY[/cells per thread] (default: autotune)")
     ap.add_argument("--quick", action="store_true", help="skip FP64, accuracy and CPU legs")
     ap.add_argument("--accuracy", action="store_true",
                     help="run the cfg3 accuracy study instead of the benchmark")

@@ -40,7 +40,7 @@ class WbError(RuntimeError):
 class WbConfig(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int32) for n in (
         "nx", "ny", "order", "basis", "bc_x", "bc_y", "eq_kind", "llf_speed", "limiter",
-        "precision", "integrator", "tile_x", "tile_y", "device", "riemann", "reserved")] + [
+        "precision", "integrator", "tile_x", "tile_y", "device", "riemann", "cells_per_thread")] + [
         (n, ctypes.c_double) for n in (
             "gamma", "gx", "gy", "rho0", "p0", "kpoly", "lx", "ly", "lim_norm", "lim_M",
             "lim_tol", "cfl", "pos_eps")]
@@ -89,7 +89,7 @@ def lib():
             "wb_norms": ([p, p, p, p, p], i32), "wb_write_dat": ([p, ctypes.c_char_p, i32], i32),
             "wb_conserved_sums": ([p, p], i32), "wb_get_stream": ([p, p], i32),
             "wb_profile_stages": ([p, i32], i32), "wb_stage_stats": ([p, p, p], i32),
-            "wb_autotune": ([p, i32, p, p], i32),
+            "wb_autotune": ([p, i32, p, p, p], i32),
             "wb_batch_create": ([p, i32, p], i32), "wb_batch_destroy": ([p], i32),
             "wb_batch_last_error": ([p], ctypes.c_char_p),
             "wb_batch_init_perturbation": ([p, p], i32), "wb_batch_step": ([p, i32, d], i32),
@@ -453,11 +453,14 @@ class Solver:
         return p.value or 0
 
     def autotune(self, steps=3):
-        """Pick the fastest compiled tile shape for this grid (state is preserved)."""
+        """Pick the fastest compiled tile shape and cells per thread for this grid (state
+        is preserved); returns (tile_x, tile_y, cells_per_thread)."""
         tx = ctypes.c_int32()
         ty = ctypes.c_int32()
-        self._check(lib().wb_autotune(self._ctx, int(steps), ctypes.byref(tx), ctypes.byref(ty)))
-        return tx.value, ty.value
+        cpt = ctypes.c_int32()
+        self._check(lib().wb_autotune(self._ctx, int(steps), ctypes.byref(tx), ctypes.byref(ty),
+                                      ctypes.byref(cpt)))
+        return tx.value, ty.value, cpt.value
 
     def profile_stages(self, on=True):
         self._check(lib().wb_profile_stages(self._ctx, 1 if on else 0))
@@ -576,11 +579,12 @@ class Batch:
         self._check(lib().wb_batch_step(self._b, int(nsteps), float(dt)))
 
     def autotune(self, reps=3):
-        """Pick the tile shape of every (degree, size class) group by timing; returns
-        {(degree, size_class): (TX, TY)} (size class 0: max(nx, ny) < 128)."""
-        t = np.zeros(12, dtype=np.int32)
+        """Pick the tile shape and cells per thread of every (degree, size class) group by
+        timing; returns {(degree, size_class): (TX, TY, CPT)} (size class 0: max(nx, ny) <
+        128)."""
+        t = np.zeros(18, dtype=np.int32)
         self._check(lib().wb_batch_autotune(self._b, int(reps), _ptr(t)))
-        return {(k, c): (int(t[(2 * k + c) * 2]), int(t[(2 * k + c) * 2 + 1]))
+        return {(k, c): tuple(int(v) for v in t[(2 * k + c) * 3:(2 * k + c) * 3 + 3])
                 for k in range(3) for c in range(2)}
 
     def sync(self):

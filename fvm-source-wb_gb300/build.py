@@ -21,27 +21,49 @@ GEN = os.path.join(OUT, "gen")
 
 
 def stage_instances():
-    """The lines of csrc/wb_stage_instances.h: (P, R, K, BT, B, TX, TY, POS)."""
+    """The lines of WB_STAGE_INSTANCES (csrc/wb_stage_instances.h):
+    (P, R, K, BT, B, TX, TY, VAR, CPT)."""
     txt = open(os.path.join(CSRC, "wb_stage_instances.h")).read()
-    pat = r"X\((\w+), (\w+), (\d), (\w), (\d), (\d+), (\d+), (\d)\)"
+    pat = r"X\((f\d+), (\w+), (\d), (\w), (\d), (\d+), (\d+), (\d), (\d)\)"
     return re.findall(pat, txt)
 
 
+def batch_instances():
+    """The lines of WB_BATCH_INSTANCES: (K, TX, TY, POS, CPT)."""
+    txt = open(os.path.join(CSRC, "wb_stage_instances.h")).read()
+    return re.findall(r"X\((\d), (\d+), (\d+), (\d), (\d)\)", txt)
+
+
+def _write_unit(name, body):
+    path = os.path.join(GEN, name)
+    if not os.path.exists(path) or open(path).read() != body:
+        with open(path, "w") as f:
+            f.write(body)
+    return path
+
+
 def generate_stage_units():
-    """One translation unit per compiled stage kernel (so nvcc runs them in parallel)."""
+    """One translation unit per compiled stage kernel and per batched stage kernel (so
+    nvcc runs them in parallel)."""
     os.makedirs(GEN, exist_ok=True)
     names = []
     for inst in stage_instances():
-        P, R, K, BT, B, TX, TY, POS = inst
-        name = "stage_%s_k%s%s_%sx%s_%s.cu" % (P, K, BT, TX, TY, POS)
-        body = ('// generated by build.py from wb_stage_instances.h\n'
-                '#include "wb_stage_launch.cuh"\n'
-                'WB_STAGE_INSTANCE(%s)\n' % ", ".join(inst))
-        path = os.path.join(GEN, name)
-        if not os.path.exists(path) or open(path).read() != body:
-            with open(path, "w") as f:
-                f.write(body)
-        names.append(path)
+        P, R, K, BT, B, TX, TY, VAR, CPT = inst
+        name = "stage_%s_k%s%s_%sx%s_%s_c%s.cu" % (P, K, BT, TX, TY, VAR, CPT)
+        names.append(_write_unit(name, '// generated by build.py from wb_stage_instances.h\n'
+                                       '#include "wb_stage_launch.cuh"\n'
+                                       'WB_STAGE_INSTANCE(%s)\n' % ", ".join(inst)))
+    for inst in batch_instances():
+        K, TX, TY, POS, CPT = inst
+        name = "batch_k%s_%sx%s_%s_c%s.cu" % (K, TX, TY, POS, CPT)
+        names.append(_write_unit(name, '// generated by build.py from wb_stage_instances.h\n'
+                                       '#include "wb_batch_launch.cuh"\n'
+                                       'WB_BATCH_INSTANCE(%s)\n' % ", ".join(inst)))
+    # units of instances no longer listed are not linked
+    keep = {os.path.basename(n) for n in names}
+    for f in os.listdir(GEN):
+        if f.endswith(".cu") and f not in keep:
+            os.remove(os.path.join(GEN, f))
     return names
 
 
@@ -77,6 +99,10 @@ def build(force=False, verbose=False):
     # slowest units first: the generated stage kernels, then the rest
     srcs = generate_stage_units() + SOURCES
     srcs.sort(key=lambda p: 0 if "_k2" in p else 1)
+    keep = {os.path.basename(p).rsplit(".", 1)[0] + ".o" for p in srcs}
+    for f in os.listdir(OUT):  # objects of units no longer built are not linked
+        if f.endswith(".o") and f not in keep:
+            os.remove(os.path.join(OUT, f))
     jobs = max(2, min(len(srcs), os.cpu_count() or 8))
     with cf.ThreadPoolExecutor(max_workers=jobs) as ex:
         results = list(ex.map(lambda s: _compile(s, force), srcs))

@@ -28,15 +28,16 @@ struct wb_batch {
   int4 *items = nullptr;  // all items, one contiguous range per group
   int nitems = 0;
   size_t items_cap = 0;
-  // A group = the items of one degree K on one tile shape, launched by its own kernel.
+  // A group = the items of one degree K on one tile shape (and cells per thread),
+  // launched by its own kernel.
   struct Group {
-    int K, TX, TY, off, count, buf;
+    int K, TX, TY, CPT, off, count, buf;
     size_t smem;
   };
   std::vector<Group> groups;
   // Tile of each instance: pinned by its config, or the choice for its (degree, size class)
-  std::vector<int> pin_tx, pin_ty, size_class;
-  int choice[3][2][2] = {{{32, 8}, {32, 8}}, {{32, 8}, {32, 8}}, {{32, 8}, {32, 8}}};
+  std::vector<int> pin_tx, pin_ty, pin_cpt, size_class;
+  int choice[3][2][3] = {{{32, 8, 1}, {32, 8, 1}}, {{32, 8, 1}, {32, 8, 1}}, {{32, 8, 1}, {32, 8, 1}}};
   int pos = 0;                        // some instance runs the positivity limiter
   StageArgs<float> *args = nullptr;  // [6 phases][2 stages][n]
   const float **state_ptrs = nullptr;  // [6 phases][n] current state per phase
@@ -86,55 +87,62 @@ int build_args(wb_batch *b, int dt_mode, double dt) {
   return WB_OK;
 }
 
-// One launch per group and stage; every stage-1 launch precedes every stage-2 launch
-// (stream order), and launches of different groups touch disjoint instances.
+// One launch for the step's start (every instance's time step), then one launch per group
+// and stage; every stage-1 launch precedes every stage-2 launch (stream order), and
+// launches of different groups touch disjoint instances.
 int launch_phase(wb_batch *b, int p) {
   const int n = (int)b->inst.size();
   int grid = 0;
+  BCK(launch_batch_begin_step(b->args + ((size_t)p * 2 + 0) * n, n, b->stream));
   for (int st = 0; st < 2; ++st)
     for (const wb_batch::Group &g : b->groups)
       BCK(launch_batch_stage(b->args + ((size_t)p * 2 + st) * n, b->items + g.off, g.count, g.buf,
-                             g.smem, b->pos, g.K, g.TX, g.TY, &grid, b->stream));
+                             g.smem, b->pos, g.K, g.TX, g.TY, g.CPT, &grid, b->stream));
   return WB_OK;
 }
 
 // Size class of an instance for the tile choice: small grids (side < 128) and the rest.
 int size_class_of(const wb_config &c) { return std::max(c.nx, c.ny) < 128 ? 0 : 1; }
 
-void instance_tile(const wb_batch *b, int i, int *tx, int *ty) {
+void instance_tile(const wb_batch *b, int i, int *tx, int *ty, int *cpt) {
   if (b->pin_tx[i] > 0) {
     *tx = b->pin_tx[i];
     *ty = b->pin_ty[i];
+    *cpt = b->pin_cpt[i];
   } else {
     const int *t = b->choice[b->cfgs[i].order][b->size_class[i]];
     *tx = t[0];
     *ty = t[1];
+    *cpt = t[2];
   }
 }
 
-// Items and groups of the instances `sel` (each on tile instance_tile, or on tx x ty when
-// given), appended to items / groups.
-void make_items(const wb_batch *b, const std::vector<int> &sel, int ftx, int fty,
+// Items and groups of the instances `sel` (each on tile instance_tile, or on tx x ty at
+// fcpt cells per thread when given), appended to items / groups.
+void make_items(const wb_batch *b, const std::vector<int> &sel, int ftx, int fty, int fcpt,
                 std::vector<int4> &items, std::vector<wb_batch::Group> &groups) {
   struct Key {
-    int K, TX, TY, i;
+    int K, TX, TY, CPT, i;
   };
   std::vector<Key> keys;
   for (int i : sel) {
-    int tx = ftx, ty = fty;
-    if (tx <= 0) instance_tile(b, i, &tx, &ty);
-    keys.push_back({b->cfgs[i].order, tx, ty, i});
+    int tx = ftx, ty = fty, cpt = fcpt;
+    if (tx <= 0) instance_tile(b, i, &tx, &ty, &cpt);
+    keys.push_back({b->cfgs[i].order, tx, ty, cpt, i});
   }
   // degree 2 first (the costliest launches start first), then by tile shape
   std::stable_sort(keys.begin(), keys.end(), [](const Key &x, const Key &y) {
-    return x.K != y.K ? x.K > y.K : (x.TX != y.TX ? x.TX > y.TX : x.TY < y.TY);
+    if (x.K != y.K) return x.K > y.K;
+    if (x.TX != y.TX) return x.TX > y.TX;
+    if (x.TY != y.TY) return x.TY < y.TY;
+    return x.CPT < y.CPT;
   });
   for (size_t k = 0; k < keys.size(); ++k) {
     const Key &q = keys[k];
     const wb_config &c = b->cfgs[q.i];
     if (groups.empty() || groups.back().K != q.K || groups.back().TX != q.TX ||
-        groups.back().TY != q.TY)
-      groups.push_back({q.K, q.TX, q.TY, (int)items.size(), 0, 0, 0});
+        groups.back().TY != q.TY || groups.back().CPT != q.CPT)
+      groups.push_back({q.K, q.TX, q.TY, q.CPT, (int)items.size(), 0, 0, 0});
     wb_batch::Group &g = groups.back();
     for (int j0 = 0; j0 < c.ny; j0 += q.TY)
       for (int i0 = 0; i0 < c.nx; i0 += q.TX) {
@@ -169,7 +177,7 @@ int build_worklist(wb_batch *b) {
   for (size_t i = 0; i < all.size(); ++i) all[i] = (int)i;
   std::vector<int4> items;
   std::vector<wb_batch::Group> groups;
-  make_items(b, all, 0, 0, items, groups);
+  make_items(b, all, 0, 0, 0, items, groups);
   int rc = upload_items(b, items);
   if (rc) return rc;
   b->nitems = (int)items.size();
@@ -226,8 +234,11 @@ int wb_batch_create(const wb_config *cfgs, int32_t n, wb_batch **out) {
         c.basis != WB_BASIS_P)
       return berr(b, WB_ERR_CONFIG,
                   "batch instances must be FP32-perturbation, SSP-RK2, total-degree basis, one device");
-    if (c.tile_x > 0 && !batch_tile_supported(c.tile_x, c.tile_y))
-      return berr(b, WB_ERR_CONFIG, "batch tiles are 32x8 or 16x16 (or 0: chosen by the batch)");
+    if (c.tile_x > 0 &&
+        !batch_tile_supported(c.order, c.tile_x, c.tile_y, c.cells_per_thread > 0 ? c.cells_per_thread : 1))
+      return berr(b, WB_ERR_CONFIG,
+                  "batch tiles are 32x8 or 16x16 at one cell per thread, 32x16 at two, 32x32 at four "
+                  "(degree 0), or 0: chosen by the batch");
     if (c.riemann != WB_RIEMANN_LLF)
       return berr(b, WB_ERR_CONFIG, "the batch runs the LLF flux");
   }
@@ -237,10 +248,12 @@ int wb_batch_create(const wb_config *cfgs, int32_t n, wb_batch **out) {
     wb_config c = cfgs[i];
     b->pin_tx.push_back(c.tile_x > 0 ? c.tile_x : 0);
     b->pin_ty.push_back(c.tile_x > 0 ? c.tile_y : 0);
+    b->pin_cpt.push_back(c.tile_x > 0 ? (c.cells_per_thread > 0 ? c.cells_per_thread : 1) : 0);
     b->size_class.push_back(size_class_of(c));
     if (c.tile_x <= 0) {  // the instance context's own tile is not used by the batch
       c.tile_x = 32;
       c.tile_y = 8;
+      c.cells_per_thread = 1;
     }
     wb_ctx *ctx = nullptr;
     int rc = wb_create(&c, &ctx);
@@ -319,10 +332,12 @@ int wb_batch_autotune(wb_batch *b, int32_t reps, int32_t *tiles) {
   if (rc) return rc;
   const int n = (int)b->inst.size();
   // Candidates are timed on stage-1 launches of the current phase.  Stage 1 writes only
-  // the buffer its real launch overwrites next and the next-parity time and speed slots,
-  // which that launch rewrites too, so the instances' states are not changed.
+  // the buffer its real launch overwrites next; the step start before them writes the
+  // phase's time step and the next-parity time and speed slots, which the real step
+  // rewrites with the same values, so the instances' states are not changed.
   const StageArgs<float> *a1 = b->args + ((size_t)b->phase * 2 + 0) * n;
-  static const int cand[2][2] = {{32, 8}, {16, 16}};
+  BCK(launch_batch_begin_step(a1, n, b->stream));
+  int cand[16][3];
   // The candidates' items go through the work-list buffer, which a captured graph reads
   // (and which may be reallocated): the graph goes first.
   if (b->graph) {
@@ -342,18 +357,19 @@ int wb_batch_autotune(wb_batch *b, int32_t reps, int32_t *tiles) {
       for (int i = 0; i < n; ++i)
         if (b->pin_tx[i] == 0 && b->cfgs[i].order == K && b->size_class[i] == cls) sel.push_back(i);
       if (sel.empty()) continue;
+      const int ncand = batch_tile_candidates(K, cand, 16);
       float best = 0.f;
-      for (int c = 0; c < 2 && !rc; ++c) {
+      for (int c = 0; c < ncand && !rc; ++c) {
         std::vector<int4> items;
         std::vector<wb_batch::Group> groups;
-        make_items(b, sel, cand[c][0], cand[c][1], items, groups);
+        make_items(b, sel, cand[c][0], cand[c][1], cand[c][2], items, groups);
         if ((rc = upload_items(b, items))) break;
         float ms = 0.f;
         for (int r = 0; r <= reps && !rc; ++r) {  // launch 0 warms up
           if (r == 1 && cudaEventRecord(e0, b->stream) != cudaSuccess) rc = WB_ERR_CUDA;
           for (const wb_batch::Group &g : groups)
             if (!rc && launch_batch_stage(a1, b->items + g.off, g.count, g.buf, g.smem, b->pos,
-                                          g.K, g.TX, g.TY, nullptr, b->stream) != cudaSuccess)
+                                          g.K, g.TX, g.TY, g.CPT, nullptr, b->stream) != cudaSuccess)
               rc = berr(b, WB_ERR_CUDA, "autotune launch failed");
         }
         if (rc) break;
@@ -366,6 +382,7 @@ int wb_batch_autotune(wb_batch *b, int32_t reps, int32_t *tiles) {
           best = ms;
           b->choice[K][cls][0] = cand[c][0];
           b->choice[K][cls][1] = cand[c][1];
+          b->choice[K][cls][2] = cand[c][2];
         }
       }
     }
@@ -378,8 +395,9 @@ int wb_batch_autotune(wb_batch *b, int32_t reps, int32_t *tiles) {
   if (tiles)
     for (int K = 0; K < 3; ++K)
       for (int cls = 0; cls < 2; ++cls) {
-        tiles[(K * 2 + cls) * 2 + 0] = b->choice[K][cls][0];
-        tiles[(K * 2 + cls) * 2 + 1] = b->choice[K][cls][1];
+        tiles[(K * 2 + cls) * 3 + 0] = b->choice[K][cls][0];
+        tiles[(K * 2 + cls) * 3 + 1] = b->choice[K][cls][1];
+        tiles[(K * 2 + cls) * 3 + 2] = b->choice[K][cls][2];
       }
   return WB_OK;
 }

@@ -14,38 +14,42 @@ __device__ __forceinline__ void unpack_item(int4 w, int &K, int &TX, int &TY) {
   TY = w.w & 0xfff;
 }
 
-// Stage the item `w` of degree K (instance arguments copied to sA, tile staged into buf).
-template <typename R, int K, int TX, int TY>
+// Stage the item `w` of degree K (instance arguments copied to sA, tile staged into buf)
+// with NT threads.
+template <typename R, int K, int TX, int TY, int NT>
 __device__ __forceinline__ void item_load(const StageArgs<R> *__restrict__ args, const int4 w,
-                                          StageArgs<R> &sA, double &sdt, R *buf, int tid,
-                                          int nthr) {
+                                          StageArgs<R> &sA, double &sdt, R *buf, int tid) {
+  constexpr int nthr = NT;
   static_assert(sizeof(StageArgs<R>) % 4 == 0, "word copy");
   const int *src = reinterpret_cast<const int *>(args + w.x);
   for (int k = tid; k < (int)(sizeof(StageArgs<R>) / 4); k += nthr)
     reinterpret_cast<int *>(&sA)[k] = src[k];
   const StageArgs<R> &A = args[w.x];
-  // the item's time step, once per item (FP64 divisions are slow on this part)
-  if (tid == 0) sdt = stage_dt(A);
+  // the instance's time step (k_batch_begin_step computed it once per step), staged with
+  // the tile
+  if (tid == 0) cp_async<8>(&sdt, &A.dev->dt[A.parity]);
   const bool lim = A.limiter == 1 && A.lim_y && K >= 1;
-  tile_load_async<R, K, 1, TX, TY>(A, lim, w.y, w.z, buf, tid);
+  tile_load_async<R, K, 1, TX, TY, NT>(A, lim, w.y, w.z, buf, tid);
 }
 
 // Resident CTAs per SM the degree-K batch kernel is compiled for (register budget
 // 65536 / (256 x this)); its shared memory (two staged tiles + the face fluxes) allows it.
 __host__ __device__ constexpr int batch_min_blocks(int K) { return K == 0 ? 4 : K == 1 ? 3 : 2; }
 
-// Persistent batched stage for the items of one group (degree K, TX x TY tiles): CTAs
-// stride over the group's work list; the next item is staged (cp.async) while the
-// current one is computed.  bufsz = the largest tile buffer of the group.  One kernel per
-// degree gives each its own register budget (and occupancy) and no runtime dispatch on K.
-template <typename R, int K, int TX, int TY, bool POS>
-__global__ void __launch_bounds__(TX * TY, batch_min_blocks(K))
+// Persistent batched stage for the items of one group (degree K, TX x TY tiles, CPT cells
+// per thread): CTAs stride over the group's work list; the next item is staged (cp.async)
+// while the current one is computed.  bufsz = the largest tile buffer of the group.  One
+// kernel per degree gives each its own register budget (and occupancy) and no runtime
+// dispatch on K.
+template <typename R, int K, int TX, int TY, bool POS, int CPT>
+__global__ void __launch_bounds__(TX * TY / CPT, batch_min_blocks(K))
     k_batch_stage(const StageArgs<R> *__restrict__ args, const int4 *__restrict__ items, int nitems,
                   int bufsz) {
+  constexpr int NT = TX * TY / CPT;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ __align__(16) StageArgs<R> sA[2];  // instance arguments of the staged items
   __shared__ double sdt[2];                     // and their time steps
-  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int tid = threadIdx.x;
   double *red = reinterpret_cast<double *>(smem_raw);
   R *bufs = reinterpret_cast<R *>(smem_raw + 64 * sizeof(double));
   R *flux = bufs + 2 * bufsz;
@@ -53,31 +57,44 @@ __global__ void __launch_bounds__(TX * TY, batch_min_blocks(K))
   // frees the previous item's buffer, argument slot and flux area (as in k_stage).
   const int G = gridDim.x;
   int it = blockIdx.x;
-  if (it < nitems) item_load<R, K, TX, TY>(args, items[it], sA[0], sdt[0], bufs, tid, nthr);
+  if (it < nitems) item_load<R, K, TX, TY, NT>(args, items[it], sA[0], sdt[0], bufs, tid);
   cp_async_commit();
   for (int k = 0; it < nitems; it += G, ++k) {
     cp_async_wait<0>();
     __syncthreads();
     if (it + G < nitems)
-      item_load<R, K, TX, TY>(args, items[it + G], sA[(k + 1) & 1], sdt[(k + 1) & 1],
-                              bufs + ((k + 1) & 1) * bufsz, tid, nthr);
+      item_load<R, K, TX, TY, NT>(args, items[it + G], sA[(k + 1) & 1], sdt[(k + 1) & 1],
+                                  bufs + ((k + 1) & 1) * bufsz, tid);
     cp_async_commit();
     const int4 w = items[it];
     const StageArgs<R> &A = sA[k & 1];
     R *buf = bufs + (k & 1) * bufsz;
     const double dt = sdt[k & 1];
-    if (A.advance_time && w.y == 0 && w.z == 0 && tid == 0) {
-      DevState *S = A.dev;
-      S->t[A.parity ^ 1] = S->t[A.parity] + dt;
-      S->nstep[A.parity ^ 1] = S->nstep[A.parity] + (dt > 0.0 ? 1 : 0);
-      S->smax[A.parity ^ 1][0] = 0ull;
-      S->smax[A.parity ^ 1][1] = 0ull;
-    }
     const bool lim = A.limiter == 1 && A.lim_y && K >= 1;
-    tile_compute<R, K, 1, TX, TY, POS ? WB_VAR_POSITIVITY : 0>(
+    tile_compute<R, K, 1, TX, TY, POS ? WB_VAR_POSITIVITY : 0, CPT>(
         A, lim, w.y, w.z, buf, flux, red, tid, dt, nullptr, false, true);
   }
   cp_async_wait<0>();
+}
+
+// Start of a step, one thread per instance: the step's time step (stage_dt, whose FP64
+// divisions are slow on this part, once per instance instead of once per work item) into
+// dev->dt[parity], and what the first stage of k_stage does for a single grid -- the next
+// time and step count, and the cleared slots of the next wave-speed maxima.  args: the
+// instances' first-stage arguments of the step.
+template <typename R>
+__global__ void __launch_bounds__(128) k_batch_begin_step(const StageArgs<R> *__restrict__ args,
+                                                          int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const StageArgs<R> &A = args[i];
+  const double dt = stage_dt(A);
+  DevState *S = A.dev;
+  S->dt[A.parity] = dt;
+  S->t[A.parity ^ 1] = S->t[A.parity] + dt;
+  S->nstep[A.parity ^ 1] = S->nstep[A.parity] + (dt > 0.0 ? 1 : 0);
+  S->smax[A.parity ^ 1][0] = 0ull;
+  S->smax[A.parity ^ 1][1] = 0ull;
 }
 
 // Per-instance wave-speed maxima of the cell means into dev->smax[parity] (the batched

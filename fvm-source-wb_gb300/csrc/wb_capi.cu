@@ -36,7 +36,7 @@ struct wb_ctx {
   cudaStream_t stream = nullptr;
   int parity = 0;
   bool speed_valid = false;
-  int TX = 32, TY = 8;
+  int TX = 32, TY = 8, CPT = 1;  // stage tile and cells per thread
   std::string err;
   bool profile = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev;  // recorded stage launches
@@ -100,12 +100,14 @@ int validate(const wb_config *c, std::string &why) {
   if (c->limiter < 0 || c->limiter > 2) return why = "bad limiter (0 off, 1 minmod, 2 positivity)", WB_ERR_CONFIG;
   if (c->limiter == 1 && !(c->lim_norm > 0.0)) return why = "lim_norm must be > 0", WB_ERR_CONFIG;
   if (c->limiter == 2 && !(c->pos_eps > 0.0)) return why = "pos_eps must be > 0", WB_ERR_CONFIG;
-  if (c->tile_x < 0 || c->tile_y < 0) return why = "bad tile", WB_ERR_CONFIG;
+  if (c->tile_x < 0 || c->tile_y < 0 || c->cells_per_thread < 0) return why = "bad tile", WB_ERR_CONFIG;
+  if (c->cells_per_thread > 0 && c->tile_x == 0)
+    return why = "cells_per_thread needs a tile (tile_x, tile_y)", WB_ERR_CONFIG;
   if (c->tile_x > 0 || c->tile_y > 0) {
-    long long t = (long long)c->tile_x * c->tile_y;
-    if (!tile_supported(c->precision == WB_PREC_FP32, c->tile_x, c->tile_y))
-      return why = "tile shape not compiled (FP32: 32x8, 16x16; FP64: 16x8, 16x4)", WB_ERR_CONFIG;
-    (void)t;
+    const int cpt = c->cells_per_thread > 0 ? c->cells_per_thread : 1;
+    if (!tile_supported(c->precision == WB_PREC_FP32, c->order, c->basis, c->tile_x, c->tile_y, cpt))
+      return why = "tile shape not compiled (FP32: 32x8, 16x16, 32x16 at 2 cells per thread, "
+                   "degree 0 also 32x32 at 4; FP64: 16x8, 16x4)", WB_ERR_CONFIG;
   }
   return WB_OK;
 }
@@ -320,14 +322,14 @@ int launch_stage_R(wb_ctx *ctx, const StageArgs<R> &A) {
   }
   // interior tiles of a state buffer are staged by TMA (tensor map for the tile the
   // launch runs)
-  int tx = ctx->TX, ty = ctx->TY;
-  stage_tile(A, ctx->cfg.order, &tx, &ty);
+  int tx = ctx->TX, ty = ctx->TY, cpt = ctx->CPT;
+  stage_tile(A, ctx->cfg.order, &tx, &ty, &cpt);
   const CUtensorMap *tm = nullptr;
   for (int b = 0; b < ctx->nbuf; ++b)
     if (A.x == (const R *)ctx->buf[b]) tm = state_tmap(ctx, A.x, tx, ty);
   StageArgs<R> B = A;
   B.use_tma = tm != nullptr;
-  CK(launch_stage(B, ctx->cfg.order, ctx->cfg.basis, ctx->TX, ctx->TY, tm, ctx->stream));
+  CK(launch_stage(B, ctx->cfg.order, ctx->cfg.basis, ctx->TX, ctx->TY, ctx->CPT, tm, ctx->stream));
   if (ctx->profile) {
     CK(cudaEventRecord(e1, ctx->stream));
     ctx->ev.emplace_back(e0, e1);
@@ -559,25 +561,32 @@ std::string tile_cache_path() {
   }
   return "tile_cache.txt";
 }
-bool tile_cache_lookup(const wb_config &c, int *tx, int *ty) {
+// lines "precision order basis nx ny tile_x tile_y cells_per_thread" (a line without the
+// last field means one cell per thread; lines naming shapes not compiled are skipped)
+bool tile_cache_lookup(const wb_config &c, int *tx, int *ty, int *cpt) {
   FILE *f = std::fopen(tile_cache_path().c_str(), "r");
   if (!f) return false;
-  int p, o, b, nx, ny, x, y;
+  char line[256];
   bool found = false;
-  while (std::fscanf(f, "%d %d %d %d %d %d %d", &p, &o, &b, &nx, &ny, &x, &y) == 7)
-    if (p == c.precision && o == c.order && b == c.basis && nx == c.nx && ny == c.ny &&
-        tile_supported(p == WB_PREC_FP32, x, y)) {
+  while (std::fgets(line, sizeof(line), f)) {
+    int p, o, b, nx, ny, x, y, k = 1;
+    const int n = std::sscanf(line, "%d %d %d %d %d %d %d %d", &p, &o, &b, &nx, &ny, &x, &y, &k);
+    if (n >= 7 && p == c.precision && o == c.order && b == c.basis && nx == c.nx &&
+        ny == c.ny && tile_supported(p == WB_PREC_FP32, o, b, x, y, k)) {
       *tx = x;
       *ty = y;
+      *cpt = k;
       found = true;
     }
+  }
   std::fclose(f);
   return found;
 }
-void tile_cache_store(const wb_config &c, int tx, int ty) {
+void tile_cache_store(const wb_config &c, int tx, int ty, int cpt) {
   FILE *f = std::fopen(tile_cache_path().c_str(), "a");
   if (!f) return;
-  std::fprintf(f, "%d %d %d %d %d %d %d\n", c.precision, c.order, c.basis, c.nx, c.ny, tx, ty);
+  std::fprintf(f, "%d %d %d %d %d %d %d %d\n", c.precision, c.order, c.basis, c.nx, c.ny, tx, ty,
+               cpt);
   std::fclose(f);
 }
 
@@ -715,6 +724,7 @@ int wb_create(const wb_config *cfg, wb_ctx **out) {
   if (cfg->tile_x > 0) {
     ctx->TX = cfg->tile_x;
     ctx->TY = cfg->tile_y;
+    ctx->CPT = cfg->cells_per_thread > 0 ? cfg->cells_per_thread : 1;
   } else if (is_fp32(ctx)) {
     ctx->TX = 32;
     ctx->TY = 8;
@@ -722,7 +732,7 @@ int wb_create(const wb_config *cfg, wb_ctx **out) {
     ctx->TX = 16;
     ctx->TY = 8;
   }
-  if (cfg->tile_x <= 0) tile_cache_lookup(*cfg, &ctx->TX, &ctx->TY);
+  if (cfg->tile_x <= 0) tile_cache_lookup(*cfg, &ctx->TX, &ctx->TY, &ctx->CPT);
   // basis tables (constant memory of both precisions' kernels, FP64 copy in global)
   Tab1D<double> t64[KMAX + 1];
   Tab1D<float> t32[KMAX + 1];
@@ -951,13 +961,13 @@ int wb_step(wb_ctx *ctx, int32_t nsteps, double dt) {
   return step_impl(ctx, nsteps, dt > 0.0 ? 0 : 1, dt, -1.0);
 }
 
-int wb_autotune(wb_ctx *ctx, int32_t steps, int32_t *tile_x, int32_t *tile_y) {
+int wb_autotune(wb_ctx *ctx, int32_t steps, int32_t *tile_x, int32_t *tile_y,
+                int32_t *cells_per_thread) {
   if (!ctx || steps < 1) return WB_ERR_ARG;
   CK(cudaSetDevice(ctx->cfg.device));
-  const int fp32 = is_fp32(ctx);
-  const int cand[2][2] = {{32, 8}, {16, 16}};
-  const int ncand = 2;
-  const int c64[2][2] = {{16, 8}, {16, 4}};
+  // every compiled (tile, cells per thread) of this precision, degree and basis
+  int cand[16][3];
+  const int ncand = tile_candidates(is_fp32(ctx), ctx->cfg.order, ctx->cfg.basis, cand, 16);
   // save the run so every candidate starts from the same state
   void *backup = nullptr;
   int rc = dalloc(ctx, (char **)&backup, ctx->state_bytes);
@@ -972,15 +982,16 @@ int wb_autotune(wb_ctx *ctx, int32_t steps, int32_t *tile_x, int32_t *tile_y) {
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
   float best = 0.0f;
-  int bx = ctx->TX, by = ctx->TY;
+  int bx = ctx->TX, by = ctx->TY, bc = ctx->CPT;
   for (int k = 0; k < ncand && rc == WB_OK; ++k) {
     ctx->cur = cur0;
     ctx->parity = par0;
     ctx->speed_valid = sv0;
     CK(cudaMemcpy(state_buf(ctx, 0), backup, ctx->state_bytes, cudaMemcpyDeviceToDevice));
     CK(cudaMemcpy(ctx->dev, &saved, sizeof(saved), cudaMemcpyHostToDevice));
-    ctx->TX = fp32 ? cand[k][0] : c64[k][0];
-    ctx->TY = fp32 ? cand[k][1] : c64[k][1];
+    ctx->TX = cand[k][0];
+    ctx->TY = cand[k][1];
+    ctx->CPT = cand[k][2];
     if ((rc = step_impl(ctx, 1, 1, 0.0, -1.0))) break;  // warm-up (first launch set-up)
     CK(cudaEventRecord(e0, ctx->stream));
     if ((rc = step_impl(ctx, steps, 1, 0.0, -1.0))) break;
@@ -992,6 +1003,7 @@ int wb_autotune(wb_ctx *ctx, int32_t steps, int32_t *tile_x, int32_t *tile_y) {
       best = ms;
       bx = ctx->TX;
       by = ctx->TY;
+      bc = ctx->CPT;
     }
   }
   ctx->cur = cur0;
@@ -1005,9 +1017,11 @@ int wb_autotune(wb_ctx *ctx, int32_t steps, int32_t *tile_x, int32_t *tile_y) {
   if (rc) return rc;
   ctx->TX = bx;
   ctx->TY = by;
-  tile_cache_store(ctx->cfg, bx, by);
+  ctx->CPT = bc;
+  tile_cache_store(ctx->cfg, bx, by, bc);
   if (tile_x) *tile_x = bx;
   if (tile_y) *tile_y = by;
+  if (cells_per_thread) *cells_per_thread = bc;
   return WB_OK;
 }
 
@@ -1152,9 +1166,10 @@ int wb_write_dat(wb_ctx *ctx, const char *path, int32_t var) {
                T.B[mode_deg(g.order, g.basis, m, 0)][0] * T.B[mode_deg(g.order, g.basis, m, 1)][0];
         u[v] = s;
       }
+      // w - w_eq of compute_primitive (2d/benchmark_2d_dg.f90:891-903) at rest: the
+      // pressure difference taken without the cancellation p(u_eq + d) - p_eq
       const double rho = re + u[0], vx = u[1] / rho, vy = u[2] / rho;
-      const double p = gm1 * (pe / gm1 + u[3] - 0.5 * rho * (vx * vx + vy * vy));
-      const double w[NV] = {rho - re, vx, vy, p - pe};
+      const double w[NV] = {u[0], vx, vy, gm1 * (u[3] - 0.5 * rho * (vx * vx + vy * vy))};
       fortran_1pe12_5(x, num);
       std::fprintf(f, "%s ", num);
       fortran_1pe12_5(y, num);
@@ -1316,9 +1331,10 @@ int ctx_rk2_stage_args(wb_ctx *ctx, int phase, int dt_mode, double dt, StageArgs
 }
 const float *ctx_state_f32(wb_ctx *c) { return (const float *)state_buf(c, 0); }
 DevState *ctx_dev_state(wb_ctx *c) { return c->dev; }
-void ctx_tile(wb_ctx *c, int *tx, int *ty) {
+void ctx_tile(wb_ctx *c, int *tx, int *ty, int *cpt) {
   *tx = c->TX;
   *ty = c->TY;
+  *cpt = c->CPT;
 }
 void ctx_advance(wb_ctx *c, int n) {
   c->cur = (c->cur + 2 * n) % c->nbuf;

@@ -394,8 +394,8 @@ int wb1d_write_dat(wb1d_ctx *c, const char *path, int32_t var) {
     wb::eq_combine(ep, wb::eq_factor_x(ep, x), fy, &re, &pe);
     const double *u = &d[(size_t)i * 3];
     const double rho = re + u[0], v = u[1] / rho;
-    const double p = gm1 * (pe / gm1 + u[2] - 0.5 * rho * v * v);
-    const double w[3] = {rho - re, v, p - pe};
+    // the pressure difference without the cancellation p(u_eq + d) - p_eq
+    const double w[3] = {u[0], v, gm1 * (u[2] - 0.5 * rho * v * v)};
     wb::fortran_1pe12_5(x, num);
     std::fprintf(f, "%s ", num);
     for (int k = var - 1; k < 3; ++k) {

@@ -24,17 +24,20 @@ WB_DECLARE_PRECISION_ENTRY_POINTS(float)
 WB_DECLARE_PRECISION_ENTRY_POINTS(double)
 
 // Stage kernels (wb_stage_dispatch.cu): the compiled kernel for precision, degree K,
-// basis and tile TX x TY (and the positivity limiter when the launch needs it).
-// tm: the tensor map of the staged input for the effective tile (stage_tile), or null.
-cudaError_t launch_stage(const StageArgs<float> &A, int K, int basis, int TX, int TY,
+// basis, tile TX x TY and CPT cells per thread (and the positivity limiter when the launch
+// needs it).  tm: the tensor map of the staged input for the effective tile (stage_tile),
+// or null.
+cudaError_t launch_stage(const StageArgs<float> &A, int K, int basis, int TX, int TY, int CPT,
                          const CUtensorMap *tm, cudaStream_t s);
-cudaError_t launch_stage(const StageArgs<double> &A, int K, int basis, int TX, int TY,
+cudaError_t launch_stage(const StageArgs<double> &A, int K, int basis, int TX, int TY, int CPT,
                          const CUtensorMap *tm, cudaStream_t s);
 // The tile the launch will run (variants run on the default tile of the precision).
-void stage_tile(const StageArgs<float> &A, int K, int *TX, int *TY);
-void stage_tile(const StageArgs<double> &A, int K, int *TX, int *TY);
-// Tile shapes the stage kernels are compiled for.
-bool tile_supported(int precision_fp32, int tx, int ty);
+void stage_tile(const StageArgs<float> &A, int K, int *TX, int *TY, int *CPT);
+void stage_tile(const StageArgs<double> &A, int K, int *TX, int *TY, int *CPT);
+// Tile shapes (TX, TY, cells per thread) the stage kernels are compiled for, and the list
+// of them for one precision, degree and basis (the autotuner's candidates).
+bool tile_supported(int precision_fp32, int order, int basis, int tx, int ty, int cpt);
+int tile_candidates(int precision_fp32, int order, int basis, int (*out)[3], int max);
 
 // Constant-memory basis tables of the auxiliary kernels, both precisions.
 inline cudaError_t upload_tables(const Tab1D<float> *t32, const Tab1D<double> *t64) {
@@ -53,11 +56,15 @@ cudaError_t launch_f64_to_f32(float *out, const double *in, long long n, cudaStr
 
 // batched form (FP32): persistent stage over a work list; per-instance max speed
 cudaError_t launch_batch_stage(const StageArgs<float> *args, const int4 *items, int nitems,
-                               int bufsz, size_t smem, int pos, int K, int TX, int TY,
+                               int bufsz, size_t smem, int pos, int K, int TX, int TY, int CPT,
                                int *grid_out, cudaStream_t s);
-bool batch_tile_supported(int TX, int TY);  // the tile shapes the batch kernels compile
+// the tile shapes (TX, TY, cells per thread) the batch kernels compile for degree K
+bool batch_tile_supported(int order, int tx, int ty, int cpt);
+int batch_tile_candidates(int order, int (*out)[3], int max);
 cudaError_t launch_batch_max_speed(const StageArgs<float> *args, const float *const *state,
                                    const int4 *items, int nitems, cudaStream_t s);
+// start of a step for the n instances (time step, time, step count, next speed slots)
+cudaError_t launch_batch_begin_step(const StageArgs<float> *args, int n, cudaStream_t s);
 
 }  // namespace wb
 
@@ -71,7 +78,7 @@ int ctx_rk2_stage_args(wb_ctx *c, int phase, int dt_mode, double dt, StageArgs<f
 const float *ctx_state_f32(wb_ctx *c);
 DevState *ctx_dev_state(wb_ctx *c);
 // tile shape chosen for the context
-void ctx_tile(wb_ctx *c, int *tx, int *ty);
+void ctx_tile(wb_ctx *c, int *tx, int *ty, int *cpt);
 // advance the host-side buffer rotation / parity bookkeeping by n RK2 steps
 void ctx_advance(wb_ctx *c, int n);
 // mark the fused wave-speed maxima of the current state as valid

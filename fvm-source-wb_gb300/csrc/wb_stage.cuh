@@ -584,11 +584,11 @@ __device__ __forceinline__ bool tma_tile(const int use_tma, const int nx, const 
 // the modes of the tile and a one-cell halo, the means of a two-cell halo when the
 // limiter is on, and the tile's equilibrium factors.  Boundary conditions are applied by
 // index mapping.  Warps copy whole rows (no per-element division).
-template <typename R, int K, int BASIS, int TX, int TY>
+template <typename R, int K, int BASIS, int TX, int TY, int NT = TX * TY>
 __device__ __forceinline__ void tile_load_async(const StageArgs<R> &A, const bool lim,
                                                 const int i0, const int j0, R *buf,
                                                 const int tid, const bool modes = true) {
-  constexpr int nthr = TX * TY;
+  constexpr int nthr = NT;  // threads of the CTA
   const TileLayout L = tile_layout(K, BASIS, TX, TY, lim);
   const int lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
   const int nx = A.nx, ny = A.ny;
@@ -623,46 +623,33 @@ __device__ __forceinline__ void tile_load_async(const StageArgs<R> &A, const boo
                   A.x + pl * P + (long long)gj * nx + (i0 - 4) + ch * 2);
     }
   } else {
+    // element-wise with x mapping: the one-cell ring, two cells deep in x with the limiter
+    // (the chunked copies above always cover columns i0 - 4 .. i0 + TX + 3)
+    const int xr = L.lim ? 2 : 1;
     int gc[3];
 #pragma unroll
-    for (int k = 0; k < 3; ++k) gc[k] = wrap_index(i0 + lane + 32 * k - 1, nx, A.bc_x);
+    for (int k = 0; k < 3; ++k) gc[k] = wrap_index(i0 + lane + 32 * k - xr, nx, A.bc_x);
     for (int row = warp; row < nrow; row += nwarp) {
       const int pl = row / L.RY, ry = row - pl * L.RY;
       const int gj = wrap_index(j0 + ry - 1, ny, A.bc_y);
       const R *src = A.x + pl * P + (long long)gj * nx;
-      R *dst = buf + L.su + row * PX + 3;
+      R *dst = buf + L.su + row * PX + 4 - xr;
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
         const int c = lane + 32 * k;
-        if (c < L.RX) cp_async<sizeof(R)>(dst + c, src + gc[k]);
+        if (c < TX + 2 * xr) cp_async<sizeof(R)>(dst + c, src + gc[k]);
       }
     }
   }
   if (L.lim) {
-    const int mrow = NV * L.LY;
-    if (vec) {
-      for (int k = tid; k < mrow * CPR; k += nthr) {
-        const int row = k / CPR, ch = k - row * CPR;
-        const int v = row / L.LY, ly = row - v * L.LY;
-        const int gj = wrap_index(j0 + ly - 2, ny, A.bc_y);
-        cp_async<16>(buf + L.sm + row * PX + ch * VEC,
-                     A.x + (long long)(v * L.NB) * P + (long long)gj * nx + (i0 - 4) + ch * VEC);
-      }
-    } else {
-      int gc[3];
-#pragma unroll
-      for (int k = 0; k < 3; ++k) gc[k] = wrap_index(i0 + lane + 32 * k - 2, nx, A.bc_x);
-      for (int row = warp; row < mrow; row += nwarp) {
-        const int v = row / L.LY, ly = row - v * L.LY;
-        const int gj = wrap_index(j0 + ly - 2, ny, A.bc_y);
-        const R *src = A.x + (long long)(v * L.NB) * P + (long long)gj * nx;
-        R *dst = buf + L.sm + row * PX + 2;
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          const int c = lane + 32 * k;
-          if (c < L.LX) cp_async<sizeof(R)>(dst + c, src + gc[k]);
-        }
-      }
+    // means of the second ring's rows j0 - 2 and j0 + TY + 1 (ring-1 columns)
+    constexpr int RXL = TX + 2;
+    for (int k = tid; k < NV * 2 * RXL; k += nthr) {
+      const int c = k % RXL, t = k / RXL, side = t & 1, v = t >> 1;
+      const int gj = wrap_index(side ? j0 + TY + 1 : j0 - 2, ny, A.bc_y);
+      const int gi = wrap_index(i0 - 1 + c, nx, A.bc_x);
+      cp_async<sizeof(R)>(buf + L.sm + (v * 2 + side) * PX + 3 + c,
+                          A.x + (long long)(v * L.NB) * P + (long long)gj * nx + gi);
     }
   }
   // equilibrium factors: fxv [NQ*(TX+2)] and fyv [NQ*(TY+2)] of the tile and its halo
@@ -688,11 +675,13 @@ __device__ __forceinline__ void tile_load_async(const StageArgs<R> &A, const boo
 }
 
 // Compute one staged tile: limiter, face fluxes, cell quadrature, RK combination and the
-// wave-speed reduction.  Thread tid owns cell (tid % TX, tid / TX).  With end_sync it ends
-// with a CTA barrier, after which `buf` and the flux area may be reused.  The wave speed
-// goes to speed_acc (the caller reduces later), or by warp atomics (warp_speed), or by a
-// CTA reduction and one atomic.
-template <typename R, int K, int BASIS, int TX, int TY, int VAR>
+// wave-speed reduction.  The CTA has TX * TY / CPT threads; thread tid owns the CPT cells
+// e = tid + c * (TX * TY / CPT), c < CPT, cell e at (e % TX, e / TX), and computes them one
+// after the other (the per-cell state is reused, so registers do not grow with CPT).
+// With end_sync it ends with a CTA barrier, after which `buf` and the flux area may be
+// reused.  The wave speed goes to speed_acc (the caller reduces later), or by warp atomics
+// (warp_speed), or by a CTA reduction and one atomic.
+template <typename R, int K, int BASIS, int TX, int TY, int VAR, int CPT = 1>
 __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool lim_,
                                              const int i0, const int j0, R *buf, R *flux,
                                              double *red, const int tid, const double dt,
@@ -707,16 +696,17 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
   constexpr bool PKF = !FP64 && !HLLC;                  // packed FP32 LLF faces
   using T = TC<R, K>;
   const TileLayout L = tile_layout(K, BASIS, TX, TY, lim_);
-  // RX / LX below are the stored row pitch (TX + 8); the staged ring starts at column 3
-  // (modes) and 2 (means) of each stored row
+  // RX below is the stored row pitch (TX + 8); the staged ring starts at column 3 of each
+  // stored row
   constexpr int RX = TX + 8, RY = TY + 2, RXY = RX * RY, RXL = TX + 2;
-  constexpr int LX = TX + 8, LY = TY + 4;
-  constexpr int nthr = TX * TY;
+  static_assert((TX * TY) % (32 * CPT) == 0, "whole warps of CPT cells per thread");
+  constexpr int nthr = TX * TY / CPT;  // threads of the CTA
+  constexpr int NCELL = TX * TY;
   const int nx = A.nx, ny = A.ny;
   const long long P = A.plane;
   const bool lim = lim_;
   R *su = buf + L.su + 3;
-  R *sm = buf + L.sm + 2;
+  const R *sm = buf + L.sm + 3;  // [NV][2][RX]: means of rows j0 - 2 and j0 + TY + 1
   // volume-point factors are indexed from the tile's first column / row (halo at -1)
   const R *sfxv = buf + L.eq + NQ;
   const R *sfxf = buf + L.eq + NQ * (TX + 2);
@@ -730,12 +720,16 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
 
   // 2. limiter on every staged cell (means never change, so cells are independent)
   if (lim) {
+    // neighbour means from the mode-0 planes (never written by the limiter) and, for the
+    // ring's first and last rows, from the staged second-ring rows
     for (int e = tid; e < NV * RY * RXL; e += nthr) {
       int rx = e % RXL, t1 = e / RXL, ry = t1 % RY, v = t1 / RY;
-      const R *mv = sm + v * LY * LX;
-      int c = (ry + 1) * LX + (rx + 1);
-      limit_modes<R, K, BASIS>(A, su + (v * NB) * RXY + ry * RX + rx, RXY, mv[c], mv[c - 1],
-                               mv[c + 1], mv[c - LX], mv[c + LX]);
+      const R *mp = su + (v * NB) * RXY + ry * RX + rx;  // mode 0 of cell (ry, rx)
+      const R *sd = sm + v * 2 * RX + rx;
+      const R ms = ry > 0 ? mp[-RX] : sd[0];
+      const R mn = ry < RY - 1 ? mp[RX] : sd[RX];
+      limit_modes<R, K, BASIS>(A, su + (v * NB) * RXY + ry * RX + rx, RXY, mp[0], mp[-1], mp[1],
+                               ms, mn);
     }
     __syncthreads();
   } else if (pos) {
@@ -973,12 +967,15 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
   __syncthreads();
 
   // 4. cells
-  const int tx = tid % TX, ty = tid / TX;
-  const int gi = i0 + tx, gj = j0 + ty;
-  const bool active = gi < nx && gj < ny;
   // wave-speed maxima in the kernel's precision (a maximum of floats is exact; FP64
   // arithmetic is slow on this part), widened to double only for the atomics
   R spx = R(0), spy = R(0);
+#pragma unroll 1
+  for (int cc = 0; cc < CPT; ++cc) {
+  const int ce = tid + cc * nthr;  // the thread's cc-th cell of the tile
+  const int tx = ce % TX, ty = ce / TX;
+  const int gi = i0 + tx, gj = j0 + ty;
+  const bool active = gi < nx && gj < ny;
   const R *uc = su + (ty + 1) * RX + (tx + 1);  // mode m of var v at uc[(v*NB+m)*RXY]
   R acc[NV][NB];
 #pragma unroll
@@ -990,7 +987,10 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
   // the face-flux area once the edge integrals have read it, so its loads land during the
   // volume quadrature instead of stalling the RK combination.  FP32, where the tile's
   // modes fit the flux area (not the tensor P2 basis).
-  constexpr bool UN = !FP64 && NV * NB * TX * TY <= NV * NQ * (TY * (TX + 1) + (TY + 1) * TX);
+  // (One cell per thread only: with several, the face fluxes are still being read by the
+  // thread's later cells.)
+  constexpr bool UN = CPT == 1 && !FP64 &&
+                      NV * NB * TX * TY <= NV * NQ * (TY * (TX + 1) + (TY + 1) * TX);
   const bool un = UN && A.o[0].out != nullptr && A.o[0].in[0] != nullptr;
   R *sun = flux;  // [NV*NB][TX*TY]
   auto source_edges = [&]() {
@@ -1018,10 +1018,22 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
         GT[b] = sfy[(v * NQ + b) * FYS + fb + TX];
         GB[b] = sfy[(v * NQ + b) * FYS + fb];
       }
+      // phi_a(-1) = (-1)^a phi_a(+1): the x term of mode (a, b) is phi_a(1) (FR - FL) for
+      // even a and phi_a(1) (FR + FL) for odd a, so the sums and differences are formed once
+      // per (parity, b) and shared by the modes
+      R XD[NQ], XS[NQ], YD[NQ], YS[NQ];
+#pragma unroll
+      for (int b = 0; b < NQ; ++b) {
+        XD[b] = FR[b] - FL[b];
+        XS[b] = FR[b] + FL[b];
+        YD[b] = GT[b] - GB[b];
+        YS[b] = GT[b] + GB[b];
+      }
 #pragma unroll
       for (int m = 0; m < NB; ++m) {
         int a = mode_deg(K, BASIS, m, 0), b = mode_deg(K, BASIS, m, 1);
-        acc[v][m] -= (T::Ep(a) * FR[b] - T::Em(a) * FL[b]) + (T::Ep(b) * GT[a] - T::Em(b) * GB[a]);
+        const R ex = (a & 1) ? XS[b] : XD[b], ey = (b & 1) ? YS[a] : YD[a];
+        acc[v][m] -= T::Ep(a) * ex + T::Ep(b) * ey;
       }
     }
 
@@ -1035,13 +1047,13 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
       for (int k = tid; k < NCH; k += nthr) {
         const int row = k / CPR_U, ch = k - row * CPR_U;
         const int pl = row / TY, r = row - pl * TY;
-        cp_async<16>(sun + pl * nthr + r * TX + ch * 4,
+        cp_async<16>(sun + pl * NCELL + r * TX + ch * 4,
                      in0 + pl * P + (long long)(j0 + r) * nx + i0 + ch * 4);
       }
     } else if (active) {
       const long long c0 = (long long)gj * nx + gi;
 #pragma unroll
-      for (int pl = 0; pl < NV * NB; ++pl) cp_async<sizeof(R)>(sun + pl * nthr + tid, in0 + pl * P + c0);
+      for (int pl = 0; pl < NV * NB; ++pl) cp_async<sizeof(R)>(sun + pl * NCELL + ce, in0 + pl * P + c0);
     }
     cp_async_commit();
   }
@@ -1233,7 +1245,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
 #pragma unroll
           for (int v = 0; v < NV; ++v)
 #pragma unroll
-            for (int m = 0; m < NB; ++m) w[v][m] = sun[(v * NB + m) * nthr + tid];
+            for (int m = 0; m < NB; ++m) w[v][m] = sun[(v * NB + m) * NCELL + ce];
         } else {
 #pragma unroll
         for (int v = 0; v < NV; ++v)
@@ -1278,16 +1290,17 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
         }
       if (oi == 0 && A.compute_speed) {
         // wave speed from the new cell mean of the full state
-        R r, p;
-        mean_wave_speed(A, rbar, pbar, val[0][0], val[1][0], val[2][0], val[3][0], r, p, spx, spy);
-        bool bad = !(r > R(0)) || !(p > R(0)) || !isfinite(spx) || !isfinite(spy);
-        if (A.eq_kind == 0) bad = !isfinite(spx) || !isfinite(spy);
+        R r, p, cx, cy;
+        mean_wave_speed(A, rbar, pbar, val[0][0], val[1][0], val[2][0], val[3][0], r, p, cx, cy);
+        bool bad = !(r > R(0)) || !(p > R(0)) || !isfinite(cx) || !isfinite(cy);
+        if (A.eq_kind == 0) bad = !isfinite(cx) || !isfinite(cy);
         if (bad) atomicOr(&A.dev->err, 1);
-        if (!isfinite(spx)) spx = R(0);
-        if (!isfinite(spy)) spy = R(0);
+        if (isfinite(cx)) spx = rfmax(spx, cx);
+        if (isfinite(cy)) spy = rfmax(spy, cy);
       }
     }
   }
+  }  // cells of this thread
   if (A.compute_speed) {
     if (speed_acc) {  // the caller reduces once after its last tile
       speed_acc[0] = fmax(speed_acc[0], spx);
@@ -1319,9 +1332,10 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
 // The tile shape is a compile-time parameter so all shared-memory indexing folds.
 // VAR selects compile-time variants (WB_VAR_*): the positivity limiter (limiter 2) and the
 // HLLC face flux; the default kernel carries neither.
-template <typename R, int K, int BASIS, int TX, int TY, int VAR>
-__global__ void __launch_bounds__(TX *TY, std::is_same<R, float>::value ? 2 : 1)
+template <typename R, int K, int BASIS, int TX, int TY, int VAR, int CPT>
+__global__ void __launch_bounds__(TX *TY / CPT, std::is_same<R, float>::value ? 2 : 1)
     k_stage(const __grid_constant__ StageArgs<R> A, const __grid_constant__ CUtensorMap tmap) {
+  constexpr int NT = TX * TY / CPT;  // threads: CPT cells each
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const int tid = threadIdx.x;
   const bool lim = A.limiter == 1 && A.lim_y && K >= 1;  // minmod: stage the means halo
@@ -1355,8 +1369,7 @@ __global__ void __launch_bounds__(TX *TY, std::is_same<R, float>::value ? 2 : 1)
                       ((L.buf * (int)sizeof(R)) & 127) == 0;
   bool pending[2] = {false, false};  // a TMA copy into buffer b not yet waited for
   unsigned phase[2] = {0u, 0u};
-  auto stage = [&](const int tl, const int b) {
-    const int i0 = (tl % ntx) * TX, j0 = (tl / ntx) * TY;
+  auto stage = [&](const int i0, const int j0, const int b) {
     R *buf = bufs + b * L.buf;
     const bool tma = tma_tile<TX, TY>(use_tma, nx, ny, i0, j0);
     if (tma && tid == 0) {
@@ -1364,7 +1377,7 @@ __global__ void __launch_bounds__(TX *TY, std::is_same<R, float>::value ? 2 : 1)
       tma_load_3d(buf + L.su, &tmap, i0 - 4, j0 - 1, 0, &bar[b]);
     }
     pending[b] = tma;
-    tile_load_async<R, K, BASIS, TX, TY>(A, lim, i0, j0, buf, tid, !tma);
+    tile_load_async<R, K, BASIS, TX, TY, NT>(A, lim, i0, j0, buf, tid, !tma);
   };
   bool ok = true;
   R speed[2] = {R(0), R(0)};  // this thread's wave-speed maxima over its tiles
@@ -1373,7 +1386,20 @@ __global__ void __launch_bounds__(TX *TY, std::is_same<R, float>::value ? 2 : 1)
   // copies are issued right after it and tile_compute needs no closing barrier.
   const int G = gridDim.x;
   int t = blockIdx.x;
-  if (t < ntiles) stage(t, 0);
+  // tile coordinates of t and of t + G, stepped without a division per tile
+  const int gq = G / ntx, gr = G - (G / ntx) * ntx;
+  int cx = t % ntx, cy = t / ntx;  // tile t
+  auto advance = [&](int &x, int &y) {
+    x += gr;
+    y += gq;
+    if (x >= ntx) {
+      x -= ntx;
+      ++y;
+    }
+  };
+  int nx_ = cx, ny_ = cy;  // tile t + G
+  advance(nx_, ny_);
+  if (t < ntiles) stage(cx * TX, cy * TY, 0);
   cp_async_commit();
   for (int k = 0; t < ntiles; t += G, ++k) {
     const int b = k & 1;
@@ -1388,17 +1414,20 @@ __global__ void __launch_bounds__(TX *TY, std::is_same<R, float>::value ? 2 : 1)
       }
     }
     if (__syncthreads_or(!ok)) break;
-    if (t + G < ntiles) stage(t + G, b ^ 1);
+    if (t + G < ntiles) stage(nx_ * TX, ny_ * TY, b ^ 1);
     cp_async_commit();
     R *buf = bufs + b * L.buf;
-    tile_compute<R, K, BASIS, TX, TY, VAR>(A, lim, (t % ntx) * TX, (t / ntx) * TY, buf, flux, red,
-                                           tid, dt, speed, false);
+    tile_compute<R, K, BASIS, TX, TY, VAR, CPT>(A, lim, cx * TX, cy * TY, buf, flux, red, tid,
+                                                dt, speed, false);
+    cx = nx_;
+    cy = ny_;
+    advance(nx_, ny_);
   }
   __syncthreads();  // the last tile's readers are done before the reduction reuses `red`
   // wave-speed maxima of all this CTA's tiles: one block reduction per launch
   if (A.compute_speed) {
-    const double mx = block_max((double)speed[0], red, tid, TX * TY);
-    const double my = block_max((double)speed[1], red, tid, TX * TY);
+    const double mx = block_max((double)speed[0], red, tid, NT);
+    const double my = block_max((double)speed[1], red, tid, NT);
     if (tid == 0) {
       atomicMax(&A.dev->smax[A.parity ^ 1][0], (unsigned long long)__double_as_longlong(mx));
       atomicMax(&A.dev->smax[A.parity ^ 1][1], (unsigned long long)__double_as_longlong(my));

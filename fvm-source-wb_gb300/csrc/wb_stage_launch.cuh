@@ -7,12 +7,13 @@
 
 namespace wb {
 
-template <typename R, int K, int BASIS, int TX, int TY, int VAR>
+template <typename R, int K, int BASIS, int TX, int TY, int VAR, int CPT>
 static cudaError_t launch_stage_kernel(const StageArgs<R> &A, const CUtensorMap *tm,
                                        cudaStream_t s) {
+  constexpr int NT = TX * TY / CPT;  // threads per CTA
   const int lim = A.limiter == 1 && A.lim_y && K >= 1;
   const size_t smem = stage_smem_bytes<R>(K, BASIS, TX, TY, lim);
-  auto kern = k_stage<R, K, BASIS, TX, TY, VAR>;
+  auto kern = k_stage<R, K, BASIS, TX, TY, VAR, CPT>;
   CUtensorMap none;
   std::memset(&none, 0, sizeof(none));
   static int per_sm[2] = {0, 0};  // occupancy per limiter setting, queried once
@@ -23,7 +24,7 @@ static cudaError_t launch_stage_kernel(const StageArgs<R> &A, const CUtensorMap 
       return e;
     }
     int n = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, TX * TY, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, NT, smem);
     if (e != cudaSuccess) {
       cudaGetLastError();
       return e;
@@ -36,17 +37,17 @@ static cudaError_t launch_stage_kernel(const StageArgs<R> &A, const CUtensorMap 
   const long long ntiles = (long long)((A.nx + TX - 1) / TX) * ((A.ny + TY - 1) / TY);
   long long grid = (long long)nsm * per_sm[lim];
   if (grid > ntiles) grid = ntiles;
-  kern<<<(unsigned)grid, TX * TY, smem, s>>>(A, tm ? *tm : none);
+  kern<<<(unsigned)grid, NT, smem, s>>>(A, tm ? *tm : none);
   return cudaGetLastError();
 }
 
 }  // namespace wb
 
 // One compiled stage kernel (a line of wb_stage_instances.h) and its launcher.
-#define WB_STAGE_INSTANCE(P, R, K, BT, B, TX, TY, VAR)                                      \
+#define WB_STAGE_INSTANCE(P, R, K, BT, B, TX, TY, VAR, CPT)                                 \
   namespace wb {                                                                            \
-  cudaError_t WB_STAGE_INSTANCE_NAME(P, K, BT, TX, TY, VAR)(                                 \
+  cudaError_t WB_STAGE_INSTANCE_NAME(P, K, BT, TX, TY, VAR, CPT)(                            \
       const StageArgs<R> &A, const CUtensorMap *tm, cudaStream_t s) {                       \
-    return launch_stage_kernel<R, K, B, TX, TY, VAR>(A, tm, s);                             \
+    return launch_stage_kernel<R, K, B, TX, TY, VAR, CPT>(A, tm, s);                        \
   }                                                                                         \
   }

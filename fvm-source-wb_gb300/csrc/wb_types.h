@@ -59,6 +59,7 @@ struct DevState {
   double t[2];
   unsigned long long smax[2][2];  // [parity][direction]
   long long nstep[2];
+  double dt[2];  // batched form: the time step of the step that starts at parity p
   int err;  // bit 0: non-physical cell mean; bit 1: a bounded device wait gave up
   int pad;
 };
@@ -110,13 +111,17 @@ struct StageArgs {
 // Layout of one staged tile in shared memory (offsets in elements).  Rows are stored with
 // pitch PX = TX + 8 starting at global column i0 - 4, so an x-interior row is one aligned
 // run of 16-byte chunks:
-//   su  [NV*NB][RY][PX]  modes of the tile and a one-cell halo (ring column rx at rx + 3)
-//   sm  [NV][LY][PX]     means of the tile and a two-cell halo (ring column lx at lx + 2;
-//                        limiter only)
+//   su  [NV*NB][RY][PX]  modes of the tile and a one-cell halo (ring column rx at rx + 3);
+//                        with the minmod limiter the columns of the second ring (i0 - 2 and
+//                        i0 + TX + 1, stored at 2 and TX + 5) are staged too
+//   sm  [NV][2][PX]      minmod limiter only: the means (mode 0) of rows j0 - 2 and
+//                        j0 + TY + 1 over the ring-1 columns (stored at 3 .. TX + 4); with
+//                        the mode-0 planes of su these are every neighbour mean the limiter
+//                        of the one-cell ring reads
 //   eq  fxv[NQ*(TX+2)], fxf[TX+1], fyv[NQ*(TY+2)], fyf[TY+1]  equilibrium factors (the
 //       volume-point factors cover the one-cell halo, for the positivity limiter)
 struct TileLayout {
-  int TX, TY, RX, RY, PX, RXY, LX, LY, NB, NQ, lim;
+  int TX, TY, RX, RY, PX, RXY, NB, NQ, lim;
   int su, sm, eq, buf;
 };
 __host__ __device__ inline TileLayout tile_layout(int K, int basis, int TX, int TY, int lim) {
@@ -127,14 +132,12 @@ __host__ __device__ inline TileLayout tile_layout(int K, int basis, int TX, int 
   L.RY = TY + 2;
   L.PX = TX + 8;
   L.RXY = L.PX * L.RY;
-  L.LX = TX + 4;
-  L.LY = TY + 4;
   L.NB = num_modes(K, basis);
   L.NQ = K + 1;
   L.lim = lim;
   L.su = 0;
   L.sm = NV * L.NB * L.RXY;
-  L.eq = L.sm + (lim ? NV * L.LY * L.PX : 0);
+  L.eq = L.sm + (lim ? NV * 2 * L.PX : 0);
   const int neq = L.NQ * (TX + 2) + TX + 1 + L.NQ * (TY + 2) + TY + 1;
   L.buf = (L.eq + neq + 31) & ~31;  // 128-byte aligned double buffers (TMA destinations)
   return L;

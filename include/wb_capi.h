@@ -73,7 +73,9 @@ typedef struct {
   int32_t tile_x, tile_y;/* CTA tile in cells; 0 = tuned default */
   int32_t device;        /* CUDA device ordinal */
   int32_t riemann;       /* WB_RIEMANN_LLF or WB_RIEMANN_HLLC */
-  int32_t reserved;      /* 0 */
+  int32_t cells_per_thread; /* cells each thread of the tile computes (the CTA has
+                            tile_x * tile_y / cells_per_thread threads); 0 = 1, or the
+                            tuned default when tile_x is 0 */
   double gamma;
   double gx, gy;         /* Phi = gx x + gy y */
   double rho0, p0;       /* isothermal reference state */
@@ -179,12 +181,16 @@ int wb_get_time(wb_ctx *ctx, double *t, int64_t *steps);
  * in evolve's locals and has no restart). */
 int wb_set_time(wb_ctx *ctx, double t, int64_t steps);
 
-/* Autotuner: times every compiled tile shape (CTA tile of cells) for this context's
- * precision, degree, basis and grid over `steps` steps of the current state (restored
- * afterwards), keeps the fastest and records it in the tile cache (the file named by the
- * environment variable WB_TILE_CACHE, else tile_cache.txt beside the library), which
- * wb_create consults when cfg->tile_x == 0.  No counterpart in the reference. */
-int wb_autotune(wb_ctx *ctx, int32_t steps, int32_t *tile_x, int32_t *tile_y);
+/* Autotuner: times every compiled tile shape (CTA tile of cells, and cells per thread) for
+ * this context's precision, degree, basis and grid over `steps` steps of the current state
+ * (restored afterwards), keeps the fastest and records it in the tile cache (the file named
+ * by the environment variable WB_TILE_CACHE, else tile_cache.txt beside the library), which
+ * wb_create consults when cfg->tile_x == 0.  Compiled shapes: FP32 32x8 and 16x16 at one
+ * cell per thread, 32x16 at two (total-degree basis and degree 0), 32x32 at four (degree
+ * 0); FP64 16x8 and 16x4.  The tiled loop is the per-cell work of compute_update,
+ * 2d/benchmark_2d_dg.f90:1207-1244.  No counterpart in the reference. */
+int wb_autotune(wb_ctx *ctx, int32_t steps, int32_t *tile_x, int32_t *tile_y,
+                int32_t *cells_per_thread);
 /* The context's CUDA stream (a cudaStream_t), for callers that order their own work
  * against it or time it with CUDA events.  No counterpart in the reference (serial). */
 int wb_get_stream(wb_ctx *ctx, void **stream);
@@ -241,10 +247,12 @@ int wb_read_dat(const char *path, int32_t ncols, double *values, int64_t capacit
 /* --- batched form -------------------------------------------------------------- */
 typedef struct wb_batch wb_batch;
 /* n independent instances (each its own grid, order, equilibrium, limiter), total-degree
- * basis, FP32-perturbation form, SSP-RK2, advanced together: per RK stage one persistent
- * launch per group (instances of one degree on one tile shape) over a work list of cell
- * tiles, the step sequence replayed from a CUDA graph.  An instance's tile_x/tile_y pin
- * its tile (32x8 or 16x16); 0 leaves it to the batch (32x8 until wb_batch_autotune). */
+ * basis, FP32-perturbation form, SSP-RK2, advanced together: per step one launch that
+ * computes every instance's time step, then per RK stage one persistent launch per group
+ * (instances of one degree on one tile shape) over a work list of cell tiles, the step
+ * sequence replayed from a CUDA graph.  An instance's tile_x/tile_y/cells_per_thread pin
+ * its tile (32x8 or 16x16 at one cell per thread, 32x16 at two, 32x32 at four for degree
+ * 0); 0 leaves it to the batch (32x8 until wb_batch_autotune). */
 int wb_batch_create(const wb_config *cfgs, int32_t n, wb_batch **out);
 int wb_batch_destroy(wb_batch *b);
 const char *wb_batch_last_error(const wb_batch *b);
@@ -254,9 +262,10 @@ int wb_batch_step(wb_batch *b, int32_t nsteps, double dt);
 int wb_batch_sync(wb_batch *b);
 /* Tile autotuner of the batched form: for every (degree, size class) group of instances
  * without a pinned tile -- size class 0: max(nx, ny) < 128, 1: the rest -- times `reps`
- * stage launches of each tile shape (32x8, 16x16) on those instances and keeps the
- * fastest.  The instances' states are not changed.  tiles (optional, int32[12]) receives
- * the choice (TX, TY) for degree K and class s at [(2K + s) * 2]. */
+ * stage launches of each compiled tile shape and cells per thread of that degree on those
+ * instances and keeps the fastest.  The instances' states are not changed.  tiles
+ * (optional, int32[18]) receives the choice (TX, TY, cells per thread) for degree K and
+ * class s at [(2K + s) * 3]. */
 int wb_batch_autotune(wb_batch *b, int32_t reps, int32_t *tiles);
 int wb_batch_download(wb_batch *b, int32_t index, double *delta);
 int wb_batch_total_dofs(wb_batch *b, int64_t *dofs);

@@ -28,7 +28,7 @@ static int layout(void) {
   FIELD(wb_config, bc_x); FIELD(wb_config, bc_y); FIELD(wb_config, eq_kind);
   FIELD(wb_config, llf_speed); FIELD(wb_config, limiter); FIELD(wb_config, precision);
   FIELD(wb_config, integrator); FIELD(wb_config, tile_x); FIELD(wb_config, tile_y);
-  FIELD(wb_config, device); FIELD(wb_config, riemann); FIELD(wb_config, reserved);
+  FIELD(wb_config, device); FIELD(wb_config, riemann); FIELD(wb_config, cells_per_thread);
   FIELD(wb_config, gamma); FIELD(wb_config, gx); FIELD(wb_config, gy); FIELD(wb_config, rho0);
   FIELD(wb_config, p0); FIELD(wb_config, kpoly); FIELD(wb_config, lx); FIELD(wb_config, ly);
   FIELD(wb_config, lim_norm); FIELD(wb_config, lim_M); FIELD(wb_config, lim_tol);

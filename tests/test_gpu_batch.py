@@ -50,11 +50,14 @@ def test_batch_autotune_and_pinned_tiles_keep_results(wb):
     either tile shape (chosen or pinned by the config) still advance exactly as alone."""
     cfgs, ics = wb.batch_workload(n=10, seed_base=91, nmin=24, nmax=200)
     cfgs[3].tile_x, cfgs[3].tile_y = 16, 16   # pinned
+    cfgs[5].tile_x, cfgs[5].tile_y, cfgs[5].cells_per_thread = 32, 16, 2
     with wb.Batch(cfgs) as b:
         b.init_perturbation(ics)
         b.step(2)
         tiles = b.autotune(2)
-        assert set(tiles.values()) <= {(32, 8), (16, 16)}
+        allowed = {(32, 8, 1), (16, 16, 1), (32, 16, 2), (32, 32, 4)}
+        assert set(tiles.values()) <= allowed
+        assert all(t != (32, 32, 4) for (k, _), t in tiles.items() if k > 0)
         b.step(8)
         b.autotune(1)
         b.step(3)

@@ -226,19 +226,45 @@ def test_evolve_reaches_tend(wb, orc):
     assert np.all(rel_l1_full(c, got, ref) < 1e-12)
 
 
-@pytest.mark.parametrize("precision", [0, 1])
-def test_tiles_agree(wb, precision):
-    c = base_cfg(nx=37, ny=23, order=2, basis=1, limiter=1)
-    d = random_delta(c, seed=21)
+# every compiled (tile, cells per thread) of a precision and degree (the autotuner's
+# candidates for the total-degree basis)
+TILES = {(1, 0): [(32, 8, 1), (16, 16, 1), (32, 16, 2), (32, 32, 4)],
+         (1, 1): [(32, 8, 1), (16, 16, 1), (32, 16, 2)],
+         (1, 2): [(32, 8, 1), (16, 16, 1), (32, 16, 2)],
+         (0, 0): [(16, 8, 1), (16, 4, 1)], (0, 1): [(16, 8, 1), (16, 4, 1)],
+         (0, 2): [(16, 8, 1), (16, 4, 1)]}
+
+
+@pytest.mark.parametrize("precision,order", sorted(TILES))
+@pytest.mark.parametrize("limiter", [0, 1])
+def test_tiles_agree(wb, precision, order, limiter):
+    """Results do not depend on the tile shape or the cells per thread: the compiled
+    shapes give the same state bit for bit (CFL steps, so the wave-speed reduction too)."""
+    c = base_cfg(nx=37, ny=23, order=order, basis=1, limiter=limiter)
+    d = random_delta(c, amp=5e-3, seed=21, smooth=not limiter)
     outs = []
-    tiles = [(32, 8), (16, 16)] if precision == 1 else [(16, 8), (16, 4)]
-    for tx, ty in tiles:
-        with solver(wb, c, precision, tile_x=tx, tile_y=ty) as s:
+    for tx, ty, cpt in TILES[(precision, order)]:
+        with solver(wb, c, precision, tile_x=tx, tile_y=ty, cells_per_thread=cpt) as s:
             s.upload(d)
             s.step(3, 1e-3)
-            outs.append(s.download())
-    for o in outs[1:]:
-        np.testing.assert_array_equal(o, outs[0])
+            s.step(3)
+            outs.append((s.download(), s.time()))
+    for o, t in outs[1:]:
+        np.testing.assert_array_equal(o, outs[0][0])
+        assert t == outs[0][1]
+
+
+def test_cells_per_thread_on_interior_tiles(wb, orc):
+    """Two cells per thread on a grid with TMA-staged interior tiles, against the oracle."""
+    c = base_cfg(nx=128, ny=72, order=2, basis=1, eq_kind=1, gx=0.0, gy=1.0, bc_x=0, bc_y=1,
+                 limiter=1)
+    d = random_delta(c, amp=1e-2, seed=9)
+    ref, _ = orc.run_rk2(orc_cfg(c), d, 4, 1e-3)
+    with solver(wb, c, 1, tile_x=32, tile_y=16, cells_per_thread=2) as s:
+        s.upload(d)
+        s.step(4, 1e-3)
+        got = s.download()
+    assert np.all(rel_l1_full(c, got, ref) < 1e-6)
 
 
 # Grids with interior tiles: those tiles are staged by one TMA copy (block inside the grid,

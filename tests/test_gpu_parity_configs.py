@@ -110,7 +110,8 @@ def test_cfg2_at_size_fp64(wb, orc):
         s.step(CFG2_STEPS)
         got = s.download()
         t, n = s.time()
-    np.testing.assert_allclose(got0, d0, rtol=0, atol=1e-14 * np.max(np.abs(d0)))
+    # downloads return the limited state (the minmod limiter flattens the bump's peak cells)
+    np.testing.assert_allclose(got0, orc.limit(oc, d0), rtol=0, atol=1e-14 * np.max(np.abs(d0)))
     assert n == CFG2_STEPS
     assert abs(t - tref) <= 1e-12 * tref
     assert np.all(rel_l1_full(c, got, ref) < 1e-12)
