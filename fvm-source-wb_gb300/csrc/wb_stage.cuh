@@ -993,6 +993,16 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
                       NV * NB * TX * TY <= NV * NQ * (TY * (TX + 1) + (TY + 1) * TX);
   const bool un = UN && A.o[0].out != nullptr && A.o[0].in[0] != nullptr;
   R *sun = flux;  // [NV*NB][TX*TY]
+  // With the minmod limiter on that input (SSP-RK2's U^n), the means of its one-cell ring
+  // are staged behind it, [NV][W: TY, E: TY, S: TX, N: TX], so the limiter of U^n reads
+  // every neighbour mean from shared memory (full tiles; a tile cut by the grid's edge
+  // reads them from global memory).
+  constexpr int RING = 2 * (TX + TY);
+  constexpr bool UNL = UN && K >= 1 &&
+                       NV * NB * TX * TY + NV * RING <= NV * NQ * (TY * (TX + 1) + (TY + 1) * TX);
+  const bool full = i0 + TX <= nx && j0 + TY <= ny;
+  const bool unl = UNL && un && full && A.o[0].lim[0] && A.limiter == 1;
+  R *sring = sun + NV * NB * NCELL;
   auto source_edges = [&]() {
     if constexpr (!FP64) {
       // FP32 form: the gravity source (0, -gx drho, -gy drho, -(gx m_x + gy m_y)) is linear
@@ -1042,18 +1052,44 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
     if (active) source_edges();
     __syncthreads();  // every thread is done with the face fluxes
     const R *in0 = A.o[0].in[0];
-    if (i0 + TX <= nx && j0 + TY <= ny && (nx % 4) == 0) {
-      constexpr int CPR_U = TX / 4, NCH = NV * NB * TY * CPR_U;
-      for (int k = tid; k < NCH; k += nthr) {
-        const int row = k / CPR_U, ch = k - row * CPR_U;
-        const int pl = row / TY, r = row - pl * TY;
-        cp_async<16>(sun + pl * NCELL + r * TX + ch * 4,
-                     in0 + pl * P + (long long)(j0 + r) * nx + i0 + ch * 4);
+    if (full && (nx % 4) == 0) {
+      // 16-byte chunks: a thread keeps its (row, chunk) and walks the planes
+      constexpr int CPR_U = TX / 4, PCH = TY * CPR_U, NCH = NV * NB * PCH;
+      if constexpr (nthr % PCH == 0) {
+        const int q = tid % PCH, r = q / CPR_U, ch = q - r * CPR_U;
+        const R *src = in0 + (long long)(j0 + r) * nx + i0 + ch * 4;
+        R *dst = sun + r * TX + ch * 4;
+        for (int pl = tid / PCH; pl < NV * NB; pl += nthr / PCH)
+          cp_async<16>(dst + pl * NCELL, src + pl * P);
+      } else {
+        for (int k = tid; k < NCH; k += nthr) {
+          const int row = k / CPR_U, ch = k - row * CPR_U;
+          const int pl = row / TY, r = row - pl * TY;
+          cp_async<16>(sun + pl * NCELL + r * TX + ch * 4,
+                       in0 + pl * P + (long long)(j0 + r) * nx + i0 + ch * 4);
+        }
       }
     } else if (active) {
       const long long c0 = (long long)gj * nx + gi;
 #pragma unroll
       for (int pl = 0; pl < NV * NB; ++pl) cp_async<sizeof(R)>(sun + pl * NCELL + ce, in0 + pl * P + c0);
+    }
+    if (unl) {  // the ring's means (boundary conditions by index mapping)
+      for (int k = tid; k < NV * RING; k += nthr) {
+        const int v = k / RING, e = k - v * RING;
+        int gx, gy;
+        if (e < 2 * TY) {
+          gx = e < TY ? i0 - 1 : i0 + TX;
+          gy = j0 + (e < TY ? e : e - TY);
+        } else {
+          const int f = e - 2 * TY;
+          gx = i0 + (f < TX ? f : f - TX);
+          gy = f < TX ? j0 - 1 : j0 + TY;
+        }
+        gx = wrap_index(gx, nx, A.bc_x);
+        gy = wrap_index(gy, ny, A.bc_y);
+        cp_async<sizeof(R)>(sring + k, in0 + (long long)(v * NB) * P + (long long)gy * nx + gx);
+      }
     }
     cp_async_commit();
   }
@@ -1263,6 +1299,18 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
           for (int v = 0; v < NV; ++v)
 #pragma unroll
             for (int m = 0; m < NB; ++m) w[v][m] = dl[v * NB + m];
+        } else if (unl && oi == 0 && ii == 0) {
+          // U^n's neighbour means from the staged tile (mode 0) and its staged ring
+#pragma unroll
+          for (int v = 0; v < NV; ++v) {
+            const R *m0 = sun + (v * NB) * NCELL + ce;
+            const R *rg = sring + v * RING;
+            const R mw = tx > 0 ? m0[-1] : rg[ty];
+            const R me = tx < TX - 1 ? m0[1] : rg[TY + ty];
+            const R ms = ty > 0 ? m0[-TX] : rg[2 * TY + tx];
+            const R mn = ty < TY - 1 ? m0[TX] : rg[2 * TY + TX + tx];
+            limit_modes<R, K, BASIS>(A, &w[v][0], 1, w[v][0], mw, me, ms, mn);
+          }
         } else if (o.lim[ii] && A.limiter == 1 && K >= 1) {
           int iw = wrap_index(gi - 1, nx, A.bc_x), ie = wrap_index(gi + 1, nx, A.bc_x);
           int js = wrap_index(gj - 1, ny, A.bc_y), jn = wrap_index(gj + 1, ny, A.bc_y);

@@ -16,20 +16,28 @@ static cudaError_t launch_stage_kernel(const StageArgs<R> &A, const CUtensorMap 
   auto kern = k_stage<R, K, BASIS, TX, TY, VAR, CPT>;
   CUtensorMap none;
   std::memset(&none, 0, sizeof(none));
-  static int per_sm[2] = {0, 0};  // occupancy per limiter setting, queried once
-  if (per_sm[lim] == 0) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  // The kernel's dynamic shared-memory limit is one attribute for both limiter settings:
+  // it is set once to the larger size (the minmod limiter stages the second-ring means);
+  // the occupancy is queried per setting.
+  static int per_sm[2] = {0, 0};
+  if (per_sm[0] == 0) {
+    const size_t s0 = stage_smem_bytes<R>(K, BASIS, TX, TY, 0);
+    const size_t s1 = stage_smem_bytes<R>(K, BASIS, TX, TY, K >= 1 ? 1 : 0);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(s0 > s1 ? s0 : s1));
     if (e != cudaSuccess) {
       cudaGetLastError();
       return e;
     }
-    int n = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, NT, smem);
-    if (e != cudaSuccess) {
-      cudaGetLastError();
-      return e;
+    for (int l = 0; l < 2; ++l) {
+      int n = 0;
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, NT, l ? s1 : s0);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        return e;
+      }
+      per_sm[l] = n > 0 ? n : 1;
     }
-    per_sm[lim] = n > 0 ? n : 1;
   }
   int dev = 0, nsm = 0;
   cudaGetDevice(&dev);

