@@ -30,7 +30,7 @@ __global__ void k_limit(const __grid_constant__ StageArgs<R> A, R *u) {
   constexpr int NB = num_modes(K, BASIS);
   int gi = blockIdx.x * blockDim.x + threadIdx.x, gj = blockIdx.y * blockDim.y + threadIdx.y;
   if (gi >= A.nx || gj >= A.ny || K < 1) return;
-  const long long P = A.plane, nx = A.nx;
+  const long long P = A.plane, nx = A.pitch;  // row stride
   const long long cell = gj * nx + gi;
   if (A.limiter == 2) {
     constexpr int NQ = K + 1;
@@ -73,7 +73,7 @@ __global__ void k_max_speed(const __grid_constant__ StageArgs<R> A, const R *u) 
   int gi = blockIdx.x * blockDim.x + threadIdx.x, gj = blockIdx.y * blockDim.y + threadIdx.y;
   double spx = 0.0, spy = 0.0;
   if (gi < A.nx && gj < A.ny) {
-    const long long cell = (long long)gj * A.nx + gi;
+    const long long cell = (long long)gj * A.pitch + gi;
     R rbar = R(0), pbar = R(0);
 #pragma unroll
     for (int qa = 0; qa < NQ; ++qa)
@@ -152,7 +152,7 @@ __global__ void k_init_ic(const __grid_constant__ AuxArgs A, const __grid_consta
         for (int v = 0; v < NV; ++v) acc[v][m] += 0.25 * d[v] * w;
       }
     }
-  const long long cell = (long long)gj * A.nx + gi;
+  const long long cell = (long long)gj * A.pitch + gi;
 #pragma unroll
   for (int v = 0; v < NV; ++v)
 #pragma unroll
@@ -218,7 +218,7 @@ __global__ void k_norms(const __grid_constant__ AuxArgs A, const Tab1D<double> *
 #pragma unroll
   for (int v = 0; v < NV; ++v) s1[v] = s2[v] = mx[v] = 0.0;
   if (gi < A.nx && gj < A.ny) {
-    const long long cell = (long long)gj * A.nx + gi;
+    const long long cell = (long long)gj * A.pitch + gi;
     const double area = (A.dx * A.dy) * 0.25;
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
@@ -293,7 +293,7 @@ __global__ void k_sums(const __grid_constant__ AuxArgs A, const Tab1D<double> *T
   int tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
   double s[NV] = {0.0, 0.0, 0.0, 0.0};
   if (gi < A.nx && gj < A.ny) {
-    const long long cell = (long long)gj * A.nx + gi;
+    const long long cell = (long long)gj * A.pitch + gi;
     double rbar = 0.0, pbar = 0.0;
     for (int qa = 0; qa < NQ; ++qa)
       for (int qb = 0; qb < NQ; ++qb) {

@@ -255,8 +255,9 @@ int wb_batch_create(const wb_config *cfgs, int32_t n, wb_batch **out) {
       c.tile_y = 8;
       c.cells_per_thread = 1;
     }
+    // rows padded to 16 bytes: every instance's tiles are staged in 16-byte chunks
     wb_ctx *ctx = nullptr;
-    int rc = wb_create(&c, &ctx);
+    int rc = ctx_create(&c, 4, &ctx);
     if (rc) {
       std::string m = std::string("instance ") + std::to_string(i) + ": " + wb_last_error(ctx);
       wb_destroy(ctx);

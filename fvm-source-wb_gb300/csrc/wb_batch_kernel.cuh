@@ -116,7 +116,7 @@ __global__ void __launch_bounds__(256)
     const int gi = w.y + tid % TX, gj = w.z + tid / TX;
     double spx = 0.0, spy = 0.0;
     if (gi < A.nx && gj < A.ny) {
-      const long long cell = (long long)gj * A.nx + gi;
+      const long long cell = (long long)gj * A.pitch + gi;
       R rbar = R(0), pbar = R(0);
       for (int qa = 0; qa < NQ; ++qa)
         for (int qb = 0; qb < NQ; ++qb) {

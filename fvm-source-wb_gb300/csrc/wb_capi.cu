@@ -23,7 +23,9 @@ using namespace wb;
 struct wb_ctx {
   wb_config cfg;
   int nb = 0, nq = 0, nbuf = 0;
-  long long ncell = 0, plane = 0;
+  long long ncell = 0, plane = 0;  // cells (nx * ny); elements between (var, mode) planes
+  int pitch = 0;                     // elements between rows of a plane: nx, or nx rounded up
+                                     // to 16 bytes for batch instances
   size_t esize = 0, state_bytes = 0;
   void *buf[6] = {nullptr};
   int cur = 0;
@@ -119,6 +121,7 @@ StageArgs<R> base_args(const wb_ctx *c) {
   const wb_config &g = c->cfg;
   A.nx = g.nx;
   A.ny = g.ny;
+  A.pitch = c->pitch;
   A.plane = c->plane;
   A.bc_x = g.bc_x;
   A.bc_y = g.bc_y;
@@ -167,6 +170,7 @@ AuxArgs aux_args(const wb_ctx *c) {
   const wb_config &g = c->cfg;
   A.nx = g.nx;
   A.ny = g.ny;
+  A.pitch = c->pitch;
   A.plane = c->plane;
   A.bc_x = g.bc_x;
   A.bc_y = g.bc_y;
@@ -200,6 +204,28 @@ int dalloc(wb_ctx *ctx, T **p, size_t bytes) {
     *p = nullptr;
     return set_err(ctx, WB_ERR_NOMEM, std::string("cudaMalloc(") + std::to_string(bytes) +
                                           " bytes): " + cudaGetErrorString(e));
+  }
+  return WB_OK;
+}
+
+// Copies the NV * nb planes of a state between a dense host array [plane][ny][nx] of
+// elements of es bytes and a device buffer [plane stride][ny rows of pitch elements].
+int copy_planes(wb_ctx *ctx, void *dst, const void *src, size_t es, cudaMemcpyKind kind,
+                cudaStream_t st) {
+  const int nrow = NV * ctx->nb;
+  const bool to_dev = kind == cudaMemcpyHostToDevice;
+  const size_t planeb = (size_t)ctx->plane * es, denseb = (size_t)ctx->ncell * es;
+  if (ctx->pitch == ctx->cfg.nx) {  // one 2D copy: a plane is one row
+    CK(cudaMemcpy2DAsync(dst, to_dev ? planeb : denseb, src, to_dev ? denseb : planeb, denseb, nrow,
+                         kind, st));
+    return WB_OK;
+  }
+  const size_t rowb = (size_t)ctx->cfg.nx * es, pitchb = (size_t)ctx->pitch * es;
+  for (int r = 0; r < nrow; ++r) {
+    char *d = (char *)dst + (size_t)r * (to_dev ? planeb : denseb);
+    const char *q = (const char *)src + (size_t)r * (to_dev ? denseb : planeb);
+    CK(cudaMemcpy2DAsync(d, to_dev ? pitchb : rowb, q, to_dev ? rowb : pitchb, rowb, ctx->cfg.ny,
+                         kind, st));
   }
   return WB_OK;
 }
@@ -284,10 +310,10 @@ const CUtensorMap *state_tmap(wb_ctx *ctx, const void *base, int TX, int TY) {
   const size_t es = ctx->esize;
   const int planes = NV * ctx->nb;
   auto encode = tensor_map_encoder();
-  if (encode && ((size_t)ctx->cfg.nx * es) % 16 == 0 && ((size_t)ctx->plane * es) % 16 == 0 &&
+  if (encode && ((size_t)ctx->pitch * es) % 16 == 0 && ((size_t)ctx->plane * es) % 16 == 0 &&
       TX + 8 <= 256 && TY + 2 <= 256 && planes <= 256) {
     cuuint64_t dims[3] = {(cuuint64_t)ctx->cfg.nx, (cuuint64_t)ctx->cfg.ny, (cuuint64_t)planes};
-    cuuint64_t strides[2] = {(cuuint64_t)ctx->cfg.nx * es, (cuuint64_t)ctx->plane * es};
+    cuuint64_t strides[2] = {(cuuint64_t)ctx->pitch * es, (cuuint64_t)ctx->plane * es};
     cuuint32_t box[3] = {(cuuint32_t)(TX + 8), (cuuint32_t)(TY + 2), (cuuint32_t)planes};
     cuuint32_t estr[3] = {1, 1, 1};
     CUresult r = encode(&m.map, es == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64,
@@ -496,18 +522,15 @@ int host_to_dev(wb_ctx *ctx, const double *h, int layout, void *dst) {
   const int nrow = NV * ctx->nb;
   const int K = ctx->cfg.order;
   if (layout == WB_LAYOUT_SOA) {
-    if (!is_fp32(ctx)) {
-      CK(cudaMemcpy2DAsync(dst, ctx->plane * sizeof(double), h, rowb, rowb, nrow,
-                           cudaMemcpyHostToDevice, ctx->stream));
-      return WB_OK;
-    }
+    if (!is_fp32(ctx)) return copy_planes(ctx, dst, h, sizeof(double), cudaMemcpyHostToDevice, ctx->stream);
     int rc = ensure_scratch(ctx);
     if (rc) return rc;
-    CK(cudaMemcpy2DAsync(ctx->scratch64, ctx->plane * sizeof(double), h, rowb, rowb, nrow,
-                         cudaMemcpyHostToDevice, ctx->stream));
+    if ((rc = copy_planes(ctx, ctx->scratch64, h, sizeof(double), cudaMemcpyHostToDevice, ctx->stream)))
+      return rc;
     CK(launch_f64_to_f32((float *)dst, ctx->scratch64, (long long)nrow * ctx->plane, ctx->stream));
     return WB_OK;
   }
+  if (ctx->pitch != ctx->cfg.nx) return set_err(ctx, WB_ERR_STATE, "Fortran layout needs unpadded rows");
   int rc = ensure_scratch(ctx);
   if (rc) return rc;
   CK(cudaMemcpyAsync(ctx->scratch64, h, rowb * nrow, cudaMemcpyHostToDevice, ctx->stream));
@@ -532,10 +555,9 @@ int dev_to_host(wb_ctx *ctx, const void *src, int layout, double *h) {
         CK(launch_f32_to_f64(ctx->scratch64, (const float *)src, (long long)nrow * ctx->plane, ctx->stream));
       s64 = ctx->scratch64;
     }
-    CK(cudaMemcpy2DAsync(h, rowb, s64, ctx->plane * sizeof(double), rowb, nrow,
-                         cudaMemcpyDeviceToHost, ctx->stream));
-    return WB_OK;
+    return copy_planes(ctx, h, s64, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
   }
+  if (ctx->pitch != ctx->cfg.nx) return set_err(ctx, WB_ERR_STATE, "Fortran layout needs unpadded rows");
   int rc = ensure_scratch(ctx);
   if (rc) return rc;
   // gather into the dense Fortran array held in scratch64 (src is a state buffer)
@@ -694,8 +716,13 @@ int wb_destroy(wb_ctx *ctx) {
   return WB_OK;
 }
 
-int wb_create(const wb_config *cfg, wb_ctx **out) {
-  if (!cfg || !out) return WB_ERR_ARG;
+}  // extern "C"
+
+namespace wb {
+// wb_create with the rows of every plane padded to a multiple of row_align elements (the
+// batched form's instances: 16-byte rows for its staging copies); row_align 1 is wb_create.
+int ctx_create(const wb_config *cfg, int row_align, wb_ctx **out) {
+  if (!cfg || !out || row_align < 1) return WB_ERR_ARG;
   *out = nullptr;
   std::string why;
   int rc = validate(cfg, why);
@@ -717,7 +744,8 @@ int wb_create(const wb_config *cfg, wb_ctx **out) {
   ctx->nq = K + 1;
   ctx->nb = num_modes(K, cfg->basis);
   ctx->ncell = (long long)cfg->nx * cfg->ny;
-  ctx->plane = (ctx->ncell + 63) / 64 * 64;
+  ctx->pitch = (cfg->nx + row_align - 1) / row_align * row_align;
+  ctx->plane = ((long long)ctx->pitch * cfg->ny + 63) / 64 * 64;
   ctx->esize = is_fp32(ctx) ? sizeof(float) : sizeof(double);
   ctx->state_bytes = (size_t)NV * ctx->nb * ctx->plane * ctx->esize;
   ctx->nbuf = cfg->integrator == WB_RK2 ? 3 : 5;
@@ -754,6 +782,11 @@ int wb_create(const wb_config *cfg, wb_ctx **out) {
   CK(cudaStreamSynchronize(ctx->stream));
   return WB_OK;
 }
+}  // namespace wb
+
+extern "C" {
+
+int wb_create(const wb_config *cfg, wb_ctx **out) { return ctx_create(cfg, 1, out); }
 
 int wb_upload_state(wb_ctx *ctx, const double *delta, int32_t layout) {
   if (!ctx || !delta) return WB_ERR_ARG;
@@ -791,9 +824,8 @@ int wb_download_state_raw(wb_ctx *ctx, void *delta) {
   if (!ctx || !delta) return WB_ERR_ARG;
   CK(cudaSetDevice(ctx->cfg.device));
   const size_t es = is_fp32(ctx) ? sizeof(float) : sizeof(double);
-  const size_t rowb = (size_t)ctx->ncell * es;
-  CK(cudaMemcpy2DAsync(delta, rowb, state_buf(ctx, 0), ctx->plane * es, rowb, NV * ctx->nb,
-                       cudaMemcpyDeviceToHost, ctx->stream));
+  int rc = copy_planes(ctx, delta, state_buf(ctx, 0), es, cudaMemcpyDeviceToHost, ctx->stream);
+  if (rc) return rc;
   CK(cudaStreamSynchronize(ctx->stream));
   return check_dev_err(ctx);
 }
@@ -801,15 +833,16 @@ int wb_download_state_raw(wb_ctx *ctx, void *delta) {
 int wb_upload_state_f32(wb_ctx *ctx, const float *delta) {
   if (!ctx || !delta) return WB_ERR_ARG;
   CK(cudaSetDevice(ctx->cfg.device));
-  const size_t rowb = (size_t)ctx->ncell * sizeof(float);
   const int nrow = NV * ctx->nb;
+  int rc;
   if (is_fp32(ctx)) {
-    CK(cudaMemcpy2DAsync(state_buf(ctx, 0), ctx->plane * sizeof(float), delta, rowb, rowb, nrow,
-                         cudaMemcpyHostToDevice, ctx->stream));
+    if ((rc = copy_planes(ctx, state_buf(ctx, 0), delta, sizeof(float), cudaMemcpyHostToDevice,
+                          ctx->stream)))
+      return rc;
   } else {
     float *tmp = (float *)state_buf(ctx, 1);  // free buffer, large enough for FP32
-    CK(cudaMemcpy2DAsync(tmp, ctx->plane * sizeof(float), delta, rowb, rowb, nrow,
-                         cudaMemcpyHostToDevice, ctx->stream));
+    if ((rc = copy_planes(ctx, tmp, delta, sizeof(float), cudaMemcpyHostToDevice, ctx->stream)))
+      return rc;
     CK(launch_f32_to_f64((double *)state_buf(ctx, 0), tmp, (long long)nrow * ctx->plane, ctx->stream));
   }
   ctx->speed_valid = false;
@@ -820,21 +853,20 @@ int wb_upload_state_f32(wb_ctx *ctx, const float *delta) {
 int wb_download_state_f32(wb_ctx *ctx, float *delta) {
   if (!ctx || !delta) return WB_ERR_ARG;
   CK(cudaSetDevice(ctx->cfg.device));
-  const size_t rowb = (size_t)ctx->ncell * sizeof(float);
   const int nrow = NV * ctx->nb;
   int rc;
   if (is_fp32(ctx)) {
     float *f;
     if ((rc = limited_copy<float>(ctx, &f))) return rc;
-    CK(cudaMemcpy2DAsync(delta, rowb, f, ctx->plane * sizeof(float), rowb, nrow,
-                         cudaMemcpyDeviceToHost, ctx->stream));
+    if ((rc = copy_planes(ctx, delta, f, sizeof(float), cudaMemcpyDeviceToHost, ctx->stream)))
+      return rc;
   } else {
     double *d;
     if ((rc = limited_copy<double>(ctx, &d))) return rc;
     float *tmp = (float *)state_buf(ctx, 2);
     CK(launch_f64_to_f32(tmp, d, (long long)nrow * ctx->plane, ctx->stream));
-    CK(cudaMemcpy2DAsync(delta, rowb, tmp, ctx->plane * sizeof(float), rowb, nrow,
-                         cudaMemcpyDeviceToHost, ctx->stream));
+    if ((rc = copy_planes(ctx, delta, tmp, sizeof(float), cudaMemcpyDeviceToHost, ctx->stream)))
+      return rc;
   }
   return check_dev_err(ctx);
 }
@@ -1095,12 +1127,10 @@ int wb_step_io_f32(wb_ctx *ctx, const float *in, float *out, int32_t nsteps, dou
   }
   const int k = ctx->io_k & 1;
   ++ctx->io_k;
-  const size_t rowb = (size_t)ctx->ncell * sizeof(float), pitch = ctx->plane * sizeof(float);
-  const int nrow = NV * ctx->nb;
   // 1. input: host -> staging buffer k (free once the compute stream took its last input)
   CK(cudaStreamWaitEvent(ctx->s_in, ctx->in_free[k], 0));
-  CK(cudaMemcpy2DAsync(ctx->io_in[k], pitch, in, rowb, rowb, nrow, cudaMemcpyHostToDevice,
-                       ctx->s_in));
+  int rc = copy_planes(ctx, ctx->io_in[k], in, sizeof(float), cudaMemcpyHostToDevice, ctx->s_in);
+  if (rc) return rc;
   CK(cudaEventRecord(ctx->in_ready[k], ctx->s_in));
   // 2. compute stream: take the input as the state, step, leave the limited result
   CK(cudaStreamWaitEvent(ctx->stream, ctx->in_ready[k], 0));
@@ -1108,7 +1138,7 @@ int wb_step_io_f32(wb_ctx *ctx, const float *in, float *out, int32_t nsteps, dou
                      ctx->stream));
   CK(cudaEventRecord(ctx->in_free[k], ctx->stream));
   ctx->speed_valid = false;
-  int rc = step_impl(ctx, nsteps, dt > 0.0 ? 0 : 1, dt, -1.0);
+  rc = step_impl(ctx, nsteps, dt > 0.0 ? 0 : 1, dt, -1.0);
   if (rc) return rc;
   CK(cudaStreamWaitEvent(ctx->stream, ctx->out_free[k], 0));
   CK(cudaMemcpyAsync(ctx->io_out[k], state_buf(ctx, 0), ctx->state_bytes,
@@ -1120,8 +1150,8 @@ int wb_step_io_f32(wb_ctx *ctx, const float *in, float *out, int32_t nsteps, dou
   CK(cudaEventRecord(ctx->out_ready[k], ctx->stream));
   // 3. output: staging buffer k -> host
   CK(cudaStreamWaitEvent(ctx->s_out, ctx->out_ready[k], 0));
-  CK(cudaMemcpy2DAsync(out, rowb, ctx->io_out[k], pitch, rowb, nrow, cudaMemcpyDeviceToHost,
-                       ctx->s_out));
+  if ((rc = copy_planes(ctx, out, ctx->io_out[k], sizeof(float), cudaMemcpyDeviceToHost, ctx->s_out)))
+    return rc;
   CK(cudaEventRecord(ctx->out_free[k], ctx->s_out));
   return WB_OK;
 }
@@ -1224,7 +1254,7 @@ int wb_norms(wb_ctx *ctx, wb_ctx *other, double l1[4], double linf[4], double l2
   if (!ctx) return WB_ERR_ARG;
   if (other && (other->cfg.nx != ctx->cfg.nx || other->cfg.ny != ctx->cfg.ny ||
                 other->cfg.order != ctx->cfg.order || other->cfg.basis != ctx->cfg.basis ||
-                other->cfg.device != ctx->cfg.device))
+                other->cfg.device != ctx->cfg.device || other->pitch != ctx->pitch))
     return set_err(ctx, WB_ERR_ARG, "norms need contexts with the same grid, basis and device");
   CK(cudaSetDevice(ctx->cfg.device));
   const double *b = nullptr;

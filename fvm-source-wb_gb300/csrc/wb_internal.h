@@ -3,6 +3,7 @@
 #pragma once
 #include <cuda.h>
 #include "wb_types.h"
+#include "../../include/wb_capi.h"
 
 namespace wb {
 
@@ -71,6 +72,8 @@ cudaError_t launch_batch_begin_step(const StageArgs<float> *args, int n, cudaStr
 // Context internals used by the batched form (defined in wb_capi.cu).
 struct wb_ctx;
 namespace wb {
+// wb_create with the rows of every plane padded to a multiple of row_align elements
+int ctx_create(const wb_config *cfg, int row_align, wb_ctx **out);
 // RK2 stage arguments of a context for step phase p (0..5: buffer rotation mod 3 and
 // parity mod 2, counted from the context's current position); FP32 contexts only.
 int ctx_rk2_stage_args(wb_ctx *c, int phase, int dt_mode, double dt, StageArgs<float> out[2]);

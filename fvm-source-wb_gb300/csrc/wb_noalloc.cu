@@ -135,6 +135,7 @@ extern "C" int wb_norms_device_noalloc(int32_t nx, int32_t ny, int32_t order, in
   std::memset(&A, 0, sizeof(A));
   A.nx = nx;
   A.ny = ny;
+  A.pitch = nx;
   A.plane = (long long)plane_stride;
   A.dx = lx / nx;
   A.dy = ly / ny;

@@ -591,7 +591,7 @@ __device__ __forceinline__ void tile_load_async(const StageArgs<R> &A, const boo
   constexpr int nthr = NT;  // threads of the CTA
   const TileLayout L = tile_layout(K, BASIS, TX, TY, lim);
   const int lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
-  const int nx = A.nx, ny = A.ny;
+  const int nx = A.nx, ny = A.ny, pitch = A.pitch;
   const long long P = A.plane;
   constexpr int PX = TX + 8;
   constexpr int VEC = 16 / (int)sizeof(R);  // elements per 16-byte chunk
@@ -599,10 +599,10 @@ __device__ __forceinline__ void tile_load_async(const StageArgs<R> &A, const boo
   // x-interior tile with 16-byte aligned rows: copy [i0-4, i0+TX+4) of every row in
   // 16-byte chunks (rows still BC-mapped in y); otherwise element-wise with x mapping
   const bool xin = i0 >= 4 && i0 + TX + 4 <= nx;
-  const bool vec = xin && (nx % VEC) == 0;
-  // rows only 8-byte aligned (FP32, nx even but not a multiple of 4): 8-byte chunks
+  const bool vec = xin && (pitch % VEC) == 0;
+  // rows only 8-byte aligned (FP32, an even row pitch not a multiple of 4): 8-byte chunks
   constexpr int VEC2 = 8 / (int)sizeof(R), CPR2 = PX / (VEC2 > 0 ? VEC2 : 1);
-  const bool vec2 = VEC2 == 2 && xin && (nx % 2) == 0 && (P % 2) == 0;
+  const bool vec2 = VEC2 == 2 && xin && (pitch % 2) == 0 && (P % 2) == 0;
   const int nrow = NV * L.NB * L.RY;
   if (!modes) {
     // the modes come by TMA (k_stage)
@@ -612,7 +612,7 @@ __device__ __forceinline__ void tile_load_async(const StageArgs<R> &A, const boo
       const int pl = row / L.RY, ry = row - pl * L.RY;
       const int gj = wrap_index(j0 + ry - 1, ny, A.bc_y);
       cp_async<16>(buf + L.su + row * PX + ch * VEC,
-                   A.x + pl * P + (long long)gj * nx + (i0 - 4) + ch * VEC);
+                   A.x + pl * P + (long long)gj * pitch + (i0 - 4) + ch * VEC);
     }
   } else if (vec2) {
     for (int k = tid; k < nrow * CPR2; k += nthr) {
@@ -620,7 +620,7 @@ __device__ __forceinline__ void tile_load_async(const StageArgs<R> &A, const boo
       const int pl = row / L.RY, ry = row - pl * L.RY;
       const int gj = wrap_index(j0 + ry - 1, ny, A.bc_y);
       cp_async<8>(buf + L.su + row * PX + ch * 2,
-                  A.x + pl * P + (long long)gj * nx + (i0 - 4) + ch * 2);
+                  A.x + pl * P + (long long)gj * pitch + (i0 - 4) + ch * 2);
     }
   } else {
     // element-wise with x mapping: the one-cell ring, two cells deep in x with the limiter
@@ -632,7 +632,7 @@ __device__ __forceinline__ void tile_load_async(const StageArgs<R> &A, const boo
     for (int row = warp; row < nrow; row += nwarp) {
       const int pl = row / L.RY, ry = row - pl * L.RY;
       const int gj = wrap_index(j0 + ry - 1, ny, A.bc_y);
-      const R *src = A.x + pl * P + (long long)gj * nx;
+      const R *src = A.x + pl * P + (long long)gj * pitch;
       R *dst = buf + L.su + row * PX + 4 - xr;
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
@@ -649,7 +649,7 @@ __device__ __forceinline__ void tile_load_async(const StageArgs<R> &A, const boo
       const int gj = wrap_index(side ? j0 + TY + 1 : j0 - 2, ny, A.bc_y);
       const int gi = wrap_index(i0 - 1 + c, nx, A.bc_x);
       cp_async<sizeof(R)>(buf + L.sm + (v * 2 + side) * PX + 3 + c,
-                          A.x + (long long)(v * L.NB) * P + (long long)gj * nx + gi);
+                          A.x + (long long)(v * L.NB) * P + (long long)gj * pitch + gi);
     }
   }
   // equilibrium factors: fxv [NQ*(TX+2)] and fyv [NQ*(TY+2)] of the tile and its halo
@@ -702,7 +702,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
   static_assert((TX * TY) % (32 * CPT) == 0, "whole warps of CPT cells per thread");
   constexpr int nthr = TX * TY / CPT;  // threads of the CTA
   constexpr int NCELL = TX * TY;
-  const int nx = A.nx, ny = A.ny;
+  const int nx = A.nx, ny = A.ny, pitch = A.pitch;
   const long long P = A.plane;
   const bool lim = lim_;
   R *su = buf + L.su + 3;
@@ -1052,12 +1052,12 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
     if (active) source_edges();
     __syncthreads();  // every thread is done with the face fluxes
     const R *in0 = A.o[0].in[0];
-    if (full && (nx % 4) == 0) {
+    if (full && (pitch % 4) == 0) {
       // 16-byte chunks: a thread keeps its (row, chunk) and walks the planes
       constexpr int CPR_U = TX / 4, PCH = TY * CPR_U, NCH = NV * NB * PCH;
       if constexpr (nthr % PCH == 0) {
         const int q = tid % PCH, r = q / CPR_U, ch = q - r * CPR_U;
-        const R *src = in0 + (long long)(j0 + r) * nx + i0 + ch * 4;
+        const R *src = in0 + (long long)(j0 + r) * pitch + i0 + ch * 4;
         R *dst = sun + r * TX + ch * 4;
         for (int pl = tid / PCH; pl < NV * NB; pl += nthr / PCH)
           cp_async<16>(dst + pl * NCELL, src + pl * P);
@@ -1066,11 +1066,11 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
           const int row = k / CPR_U, ch = k - row * CPR_U;
           const int pl = row / TY, r = row - pl * TY;
           cp_async<16>(sun + pl * NCELL + r * TX + ch * 4,
-                       in0 + pl * P + (long long)(j0 + r) * nx + i0 + ch * 4);
+                       in0 + pl * P + (long long)(j0 + r) * pitch + i0 + ch * 4);
         }
       }
     } else if (active) {
-      const long long c0 = (long long)gj * nx + gi;
+      const long long c0 = (long long)gj * pitch + gi;
 #pragma unroll
       for (int pl = 0; pl < NV * NB; ++pl) cp_async<sizeof(R)>(sun + pl * NCELL + ce, in0 + pl * P + c0);
     }
@@ -1088,7 +1088,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
         }
         gx = wrap_index(gx, nx, A.bc_x);
         gy = wrap_index(gy, ny, A.bc_y);
-        cp_async<sizeof(R)>(sring + k, in0 + (long long)(v * NB) * P + (long long)gy * nx + gx);
+        cp_async<sizeof(R)>(sring + k, in0 + (long long)(v * NB) * P + (long long)gy * pitch + gx);
       }
     }
     cp_async_commit();
@@ -1261,7 +1261,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
     // RK stage combination: out = sum c_i [lim](in_i) + beta Y + (cdt dt) L(Y).  The RK
     // inputs are read once and the outputs not re-read by this launch: streaming (.cs)
     // loads and stores keep them from displacing the staged halos in L1/L2.
-    const long long cell = (long long)gj * nx + gi;
+    const long long cell = (long long)gj * pitch + gi;
 #pragma unroll
     for (int oi = 0; oi < 2; ++oi) {
       const Combo<R> &o = A.o[oi];
@@ -1317,9 +1317,10 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
 #pragma unroll
           for (int v = 0; v < NV; ++v) {
             const R *m0p = in + (long long)(v * NB) * P;
-            limit_modes<R, K, BASIS>(A, &w[v][0], 1, w[v][0], m0p[(long long)gj * nx + iw],
-                                     m0p[(long long)gj * nx + ie], m0p[(long long)js * nx + gi],
-                                     m0p[(long long)jn * nx + gi]);
+            limit_modes<R, K, BASIS>(A, &w[v][0], 1, w[v][0], m0p[(long long)gj * pitch + iw],
+                                     m0p[(long long)gj * pitch + ie],
+                                     m0p[(long long)js * pitch + gi],
+                                     m0p[(long long)jn * pitch + gi]);
           }
         }
 #pragma unroll

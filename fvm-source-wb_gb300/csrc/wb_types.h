@@ -83,6 +83,7 @@ struct StageArgs {
   const R *x;                 // stage input (loaded with halo, limited if lim_y)
   Combo<R> o[2];              // o[1].out may be null
   int nx, ny;
+  int pitch;                  // elements between rows of a plane (>= nx): cell (i, j) at j*pitch + i
   long long plane;            // elements between (var, mode) planes
   int bc_x, bc_y, llf_speed, limiter, lim_y;  // limiter: 0 off, 1 minmod, 2 positivity
   int riemann;                // 0 LLF, 1 HLLC (the kernel variant must match)
@@ -157,6 +158,7 @@ __host__ __device__ inline size_t stage_smem_bytes(int K, int basis, int TX, int
 // Arguments of the per-cell auxiliary kernels (FP64 equilibrium factors).
 struct AuxArgs {
   int nx, ny;
+  int pitch;  // elements between rows of a plane (>= nx)
   long long plane;
   int bc_x, bc_y, limiter, eq_kind;
   double dx, dy, gamma, gx, gy, rho0, p0, kpoly, npoly;
