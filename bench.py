@@ -212,14 +212,32 @@ def run_reference(args):
 
 # ---------------------------------------------------------------- our arm
 
-def batch_leg(wb, n, dev, steps=24, warmup=6):
+def parse_batch_tiles(spec):
+    """'0:32x16/2,1:32x16/2,2:32x8/1' -> {degree: (TX, TY, CPT)}."""
+    out = {}
+    for part in filter(None, spec.split(",")):
+        k, shape = part.split(":")
+        dims, _, cpt = shape.lower().partition("/")
+        tx, ty = (int(v) for v in dims.split("x"))
+        out[int(k)] = (tx, ty, int(cpt or 1))
+    return out
+
+
+def batch_leg(wb, n, dev, steps=24, warmup=6, pinned=None):
     """The batched form on n instances: DOF-updates/s over `steps` CFL steps (host clock
     around graph launches + sync, after `warmup` steps that include the graph capture), and
-    its HBM roofline fraction (20 B per DOF-update per SSP-RK2 step, all stage launches)."""
+    its HBM roofline fraction (20 B per DOF-update per SSP-RK2 step, all stage launches).
+    pinned: {degree: (TX, TY, CPT)} pins those degrees' tiles (profiling); the rest are
+    autotuned."""
     cfgs, ics = wb.batch_workload(n=n, device=dev)
+    for c in cfgs:
+        if pinned and c.order in pinned:
+            c.tile_x, c.tile_y, c.cells_per_thread = pinned[c.order]
     with wb.Batch(cfgs) as bt:
         bt.init_perturbation(ics)
         tiles = bt.autotune(3)
+        if pinned:
+            tiles.update({(k, c): pinned[k] for k in pinned for c in range(2)})
         bt.step(warmup)
         bt.sync()
         t0 = time.perf_counter()
@@ -309,7 +327,8 @@ def limited_leg(wb, name, dev, steps=6, warmup=3):
 def run_batch_only(args):
     wb = load_package()
     line = {"metric": "batched form: " + UNIT, "impl": "batch"}
-    line.update(batch_leg(wb, args.batch, 0, steps=args.steps, warmup=max(args.warmup, 6)))
+    line.update(batch_leg(wb, args.batch, 0, steps=args.steps, warmup=max(args.warmup, 6),
+                          pinned=parse_batch_tiles(args.batch_tiles)))
     print(json.dumps(line))
     return 0
 
@@ -558,6 +577,8 @@ def main():
     ap.add_argument("--accuracy-steps", type=int, default=500)
     ap.add_argument("--batch", type=int, default=0,
                     help="run only the batched form with this many instances (profiling)")
+    ap.add_argument("--batch-tiles", default="",
+                    help="with --batch: pin tiles per degree, e.g. 0:32x16/2,1:32x16/2,2:32x8/1")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
