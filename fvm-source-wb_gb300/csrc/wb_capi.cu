@@ -1200,13 +1200,15 @@ int wb_write_dat(wb_ctx *ctx, const char *path, int32_t var) {
       // pressure difference taken without the cancellation p(u_eq + d) - p_eq
       const double rho = re + u[0], vx = u[1] / rho, vy = u[2] / rho;
       const double w[NV] = {u[0], vx, vy, gm1 * (u[3] - 0.5 * rho * (vx * vx + vy * vy))};
+      // fields separated by the 1X of the format; Fortran ends the record at the last
+      // field, with no trailing blank
       fortran_1pe12_5(x, num);
-      std::fprintf(f, "%s ", num);
+      std::fprintf(f, "%s", num);
       fortran_1pe12_5(y, num);
-      std::fprintf(f, "%s ", num);
+      std::fprintf(f, " %s", num);
       for (int v = var - 1; v < NV; ++v) {
         fortran_1pe12_5(w[v], num);
-        std::fprintf(f, "%s ", num);
+        std::fprintf(f, " %s", num);
       }
       std::fprintf(f, "\n");
     }

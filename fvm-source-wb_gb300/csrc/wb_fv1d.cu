@@ -396,11 +396,11 @@ int wb1d_write_dat(wb1d_ctx *c, const char *path, int32_t var) {
     const double rho = re + u[0], v = u[1] / rho;
     // the pressure difference without the cancellation p(u_eq + d) - p_eq
     const double w[3] = {u[0], v, gm1 * (u[2] - 0.5 * rho * v * v)};
-    wb::fortran_1pe12_5(x, num);
-    std::fprintf(f, "%s ", num);
+    wb::fortran_1pe12_5(x, num);  // fields separated by the format's 1X, none trailing
+    std::fprintf(f, "%s", num);
     for (int k = var - 1; k < 3; ++k) {
       wb::fortran_1pe12_5(w[k], num);
-      std::fprintf(f, "%s ", num);
+      std::fprintf(f, " %s", num);
     }
     std::fprintf(f, "\n");
   }

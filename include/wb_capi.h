@@ -233,7 +233,8 @@ int wb_norms_device_noalloc(int32_t nx, int32_t ny, int32_t order, int32_t basis
 /* Text snapshot in the reference's format: output_file, 2d/benchmark_2d_dg.f90:468-495 --
  * one line per cell (x index outer, y inner) with x, y of the cell's first Gauss point
  * and the primitive perturbation w - w_eq there for variables var..4, each written as
- * Fortran 1PE12.5 followed by one blank. */
+ * Fortran 1PE12.5, separated by one blank (the format's 1X; no blank ends a record, as
+ * Fortran writes it). */
 int wb_write_dat(wb_ctx *ctx, const char *path, int32_t var);
 /* Reads a text snapshot written in that format ('(7(1PE12.5,1X))', one record per line,
  * a record of more than 7 values continued on the next lines, 7 per line) into
@@ -293,8 +294,8 @@ int wb1d_compute_update(wb1d_ctx *c, const double *delta, double *dudt);
 int wb1d_evolve(wb1d_ctx *c, double tend, int32_t max_steps, int32_t *steps_done, double *t_out);
 /* Text snapshot of the 1D state: output_file, benchmark_1d.f90:69-100 -- one line per cell
  * with the cell centre x and the primitive perturbation w - w_eq at the centre for
- * variables var..3 of (rho, u, p) (the reference writes var = 3), each as 1PE12.5 and a
- * blank; read back with wb_read_dat. */
+ * variables var..3 of (rho, u, p) (the reference writes var = 3), each as 1PE12.5,
+ * separated by one blank; read back with wb_read_dat. */
 int wb1d_write_dat(wb1d_ctx *c, const char *path, int32_t var);
 
 #ifdef __cplusplus

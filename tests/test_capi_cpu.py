@@ -27,7 +27,13 @@ def test_exports_every_declared_symbol(wb):
 def test_config_validation_without_device(wb):
     L = wb.lib()
     bad = [dict(nx=0), dict(order=5), dict(basis=7), dict(gamma=1.0), dict(precision=3),
-           dict(eq_kind=2, kpoly=1.0, gy=10.0), dict(tile_x=7, tile_y=3)]
+           dict(eq_kind=2, kpoly=1.0, gy=10.0), dict(tile_x=7, tile_y=3),
+           # cells per thread: only with a tile, and only the compiled shapes
+           dict(cells_per_thread=2),
+           dict(precision=1, order=2, basis=1, tile_x=32, tile_y=16),
+           dict(precision=1, order=2, basis=0, tile_x=32, tile_y=16, cells_per_thread=2),
+           dict(precision=1, order=1, basis=1, tile_x=32, tile_y=32, cells_per_thread=4),
+           dict(precision=0, order=1, basis=1, tile_x=32, tile_y=16, cells_per_thread=2)]
     for kw in bad:
         c = wb.default_config(**kw)
         ctx = ctypes.c_void_p()

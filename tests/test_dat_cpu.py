@@ -2,6 +2,8 @@
 files written here: no GPU is involved.  The writers (2D output_file of
 2d/benchmark_2d_dg.f90:468-495, 1D output_file of benchmark_1d.f90:69-100) round-trip
 through it in tests/test_gpu_io.py."""
+import os
+
 import numpy as np
 import pytest
 
@@ -20,7 +22,26 @@ def write_records(path, rows):
     with open(path, "w") as f:
         for r in rows:
             for k in range(0, len(r), 7):  # 7 values per line, the descriptor's repeat count
-                f.write("".join(f1pe12_5(v) + " " for v in r[k:k + 7]) + "\n")
+                f.write(" ".join(f1pe12_5(v) for v in r[k:k + 7]) + "\n")
+
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "initwo_sample.dat")
+
+
+def test_reads_the_references_own_snapshot(wb):
+    """Records of the reference's initwo.dat (its output_file, 150 x 150 cells): the reader
+    gives what np.loadtxt -- the reader of the reference's post-processing -- gives."""
+    got = wb.read_dat(GOLDEN, 6)
+    np.testing.assert_array_equal(got, np.loadtxt(GOLDEN))
+    assert got.shape[0] >= 150 and np.any(got < 0)
+
+
+def test_format_reproduces_the_references_bytes():
+    """The 1PE12.5 formatter (the model of the writers' format in these tests) re-creates
+    every sampled record of the reference's snapshot byte for byte: right-justified
+    12-column fields, one blank between them and none at the end of the record."""
+    for ln in open(GOLDEN).read().splitlines():
+        assert ln == " ".join(f1pe12_5(float(t)) for t in ln.split()), ln
 
 
 def test_reads_what_the_format_writes(wb, tmp_path):
@@ -48,7 +69,7 @@ def test_records_longer_than_seven_values_continue_on_the_next_line(wb, tmp_path
 
 def test_nan_and_blank_lines(wb, tmp_path):
     p = tmp_path / "nan.dat"
-    p.write_text("\n" + f1pe12_5(1.0) + "          NaN \n\n" + f1pe12_5(-2.0) + f1pe12_5(3.0) + "\n")
+    p.write_text("\n" + f1pe12_5(1.0) + "          NaN\n\n" + f1pe12_5(-2.0) + " " + f1pe12_5(3.0) + "\n")
     got = wb.read_dat(str(p), 2)
     assert got.shape == (2, 2) and np.isnan(got[0, 1])
     np.testing.assert_array_equal(got[1], [-2.0, 3.0])

@@ -47,7 +47,7 @@ def test_output_file_format(wb, orc, tmp_path):
     lines = open(tmp_path / "snap.dat").read().splitlines()
     assert len(lines) == 30
     for ln in lines:
-        assert len(ln) == 6 * 13  # six values of 12 columns, each followed by a blank
+        assert len(ln) == 6 * 13 - 1  # six values of 12 columns, one blank between them
     oc = orc_cfg(c)
     nodes = orc.nodes_from_modes(oc, dl)
     x, _ = orc.gl(2)
@@ -164,6 +164,11 @@ def test_output_file_round_trip_2d(wb, orc, tmp_path, var):
         s.output_file(str(tmp_path / "snap.dat"), var=var)
         dl = s.download()
     x, y, fields = wb.read_output_file(str(tmp_path / "snap.dat"), 9, 7, var=var)
+    # byte for byte what the reference's output_file writes for these numbers (the
+    # formatter below reproduces the reference's own initwo.dat, test_dat_cpu.py)
+    from test_dat_cpu import f1pe12_5
+    for ln in open(tmp_path / "snap.dat").read().splitlines():
+        assert ln == " ".join(f1pe12_5(float(t)) for t in ln.split())
     assert x.shape == (9, 7) and len(fields) == 5 - var
     oc = orc_cfg(c)
     nodes = orc.nodes_from_modes(oc, dl)
@@ -193,7 +198,7 @@ def test_output_file_round_trip_1d(wb, orc, tmp_path, var):
         got = s.download()
         s.output_file(str(tmp_path / "snap1d.dat"), var=var)
     lines = open(tmp_path / "snap1d.dat").read().splitlines()
-    assert len(lines) == 64 and all(len(ln) == (1 + 4 - var) * 13 for ln in lines)
+    assert len(lines) == 64 and all(len(ln) == (1 + 4 - var) * 13 - 1 for ln in lines)
     x, fields = wb.Solver1D.read_output_file(str(tmp_path / "snap1d.dat"), var=var)
     re, pe = orc.fv1d_eq_cells(c)
     rho = re + got[:, 0]
