@@ -215,6 +215,11 @@ int copy_planes(wb_ctx *ctx, void *dst, const void *src, size_t es, cudaMemcpyKi
   const int nrow = NV * ctx->nb;
   const bool to_dev = kind == cudaMemcpyHostToDevice;
   const size_t planeb = (size_t)ctx->plane * es, denseb = (size_t)ctx->ncell * es;
+  if (ctx->pitch == ctx->cfg.nx && ctx->plane == ctx->ncell) {
+    // planes without padding: the state is one contiguous block on both sides
+    CK(cudaMemcpyAsync(dst, src, denseb * nrow, kind, st));
+    return WB_OK;
+  }
   if (ctx->pitch == ctx->cfg.nx) {  // one 2D copy: a plane is one row
     CK(cudaMemcpy2DAsync(dst, to_dev ? planeb : denseb, src, to_dev ? denseb : planeb, denseb, nrow,
                          kind, st));
@@ -1134,15 +1139,14 @@ int wb_step_io_f32(wb_ctx *ctx, const float *in, float *out, int32_t nsteps, dou
   CK(cudaEventRecord(ctx->in_ready[k], ctx->s_in));
   // 2. compute stream: take the input as the state, step, leave the limited result
   CK(cudaStreamWaitEvent(ctx->stream, ctx->in_ready[k], 0));
-  CK(cudaMemcpyAsync(state_buf(ctx, 0), ctx->io_in[k], ctx->state_bytes, cudaMemcpyDeviceToDevice,
-                     ctx->stream));
+  // device-side copies run on the SMs: the copy engines are busy with the host transfers
+  CK(launch_copy_device(state_buf(ctx, 0), ctx->io_in[k], ctx->state_bytes, ctx->stream));
   CK(cudaEventRecord(ctx->in_free[k], ctx->stream));
   ctx->speed_valid = false;
   rc = step_impl(ctx, nsteps, dt > 0.0 ? 0 : 1, dt, -1.0);
   if (rc) return rc;
   CK(cudaStreamWaitEvent(ctx->stream, ctx->out_free[k], 0));
-  CK(cudaMemcpyAsync(ctx->io_out[k], state_buf(ctx, 0), ctx->state_bytes,
-                     cudaMemcpyDeviceToDevice, ctx->stream));
+  CK(launch_copy_device(ctx->io_out[k], state_buf(ctx, 0), ctx->state_bytes, ctx->stream));
   if (ctx->cfg.limiter && ctx->cfg.order >= 1) {
     StageArgs<float> A = base_args<float>(ctx);
     CK(launch_limit(A, (float *)ctx->io_out[k], ctx->cfg.order, ctx->cfg.basis, ctx->stream));

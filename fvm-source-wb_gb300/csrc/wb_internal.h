@@ -54,6 +54,8 @@ cudaError_t launch_norms(const AuxArgs &A, const Tab1D<double> *Td, const double
 cudaError_t launch_f32_to_f64(double *out, const float *in, long long n, cudaStream_t s);
 cudaError_t launch_wait_selftest(int *err, int polls, cudaStream_t s);
 cudaError_t launch_f64_to_f32(float *out, const double *in, long long n, cudaStream_t s);
+// device-to-device copy on the SMs (16-byte aligned buffers, a multiple of 16 bytes)
+cudaError_t launch_copy_device(void *out, const void *in, size_t bytes, cudaStream_t s);
 
 // batched form (FP32): persistent stage over a work list; per-instance max speed
 cudaError_t launch_batch_stage(const StageArgs<float> *args, const int4 *items, int nitems,

@@ -50,4 +50,21 @@ cudaError_t launch_f64_to_f32(float *out, const double *in, long long n, cudaStr
   return cudaGetLastError();
 }
 
+// Device-to-device copy of n 16-byte words on the SMs: inside a pipeline whose host copies
+// occupy the copy engines, a cudaMemcpyAsync between device buffers would queue behind them.
+__global__ void __launch_bounds__(256) k_copy16(uint4 *__restrict__ out,
+                                                const uint4 *__restrict__ in, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    __stcs(out + i, __ldcs(in + i));
+}
+cudaError_t launch_copy_device(void *out, const void *in, size_t bytes, cudaStream_t s) {
+  if (bytes % 16 != 0 || ((uintptr_t)out | (uintptr_t)in) % 16 != 0) return cudaErrorInvalidValue;
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  k_copy16<<<nsm * 8, 256, 0, s>>>((uint4 *)out, (const uint4 *)in, (long long)(bytes / 16));
+  return cudaGetLastError();
+}
+
 }  // namespace wb
