@@ -25,6 +25,11 @@ struct wb_batch {
   std::vector<wb_config> cfgs;
   int device = 0;
   cudaStream_t stream = nullptr;
+  // one stream per group and the fork/join events that order them against `stream`: the
+  // groups advance disjoint instances, so each runs its two stages on its own branch
+  static constexpr int kMaxBranches = 8;
+  cudaStream_t branch[kMaxBranches] = {};
+  cudaEvent_t fork = nullptr, join[kMaxBranches] = {};
   int4 *items = nullptr;  // all items, one contiguous range per group
   int nitems = 0;
   size_t items_cap = 0;
@@ -87,17 +92,29 @@ int build_args(wb_batch *b, int dt_mode, double dt) {
   return WB_OK;
 }
 
-// One launch for the step's start (every instance's time step), then one launch per group
-// and stage; every stage-1 launch precedes every stage-2 launch (stream order), and
-// launches of different groups touch disjoint instances.
+// One launch for the step's start (every instance's time step), then per group its stage-1
+// and stage-2 launches.  Groups advance disjoint instances, so each group's two stages
+// run on a branch of their own (its stream, forked from and joined back to the batch
+// stream): a group's second stage waits only for its own first stage, and the groups' launch
+// tails overlap.  With more groups than branches the extra groups share the last branch.
 int launch_phase(wb_batch *b, int p) {
   const int n = (int)b->inst.size();
   int grid = 0;
   BCK(launch_batch_begin_step(b->args + ((size_t)p * 2 + 0) * n, n, b->stream));
-  for (int st = 0; st < 2; ++st)
-    for (const wb_batch::Group &g : b->groups)
+  BCK(cudaEventRecord(b->fork, b->stream));
+  const int nb = std::min((int)b->groups.size(), wb_batch::kMaxBranches);
+  for (int k = 0; k < nb; ++k) BCK(cudaStreamWaitEvent(b->branch[k], b->fork, 0));
+  for (size_t gi = 0; gi < b->groups.size(); ++gi) {
+    const wb_batch::Group &g = b->groups[gi];
+    cudaStream_t s = b->branch[std::min((int)gi, nb - 1)];
+    for (int st = 0; st < 2; ++st)
       BCK(launch_batch_stage(b->args + ((size_t)p * 2 + st) * n, b->items + g.off, g.count, g.buf,
-                             g.smem, b->pos, g.K, g.TX, g.TY, g.CPT, &grid, b->stream));
+                             g.smem, b->pos, g.K, g.TX, g.TY, g.CPT, &grid, s));
+  }
+  for (int k = 0; k < nb; ++k) {
+    BCK(cudaEventRecord(b->join[k], b->branch[k]));
+    BCK(cudaStreamWaitEvent(b->stream, b->join[k], 0));
+  }
   return WB_OK;
 }
 
@@ -218,6 +235,11 @@ int wb_batch_destroy(wb_batch *b) {
   cudaFree(b->args);
   cudaFree(b->state_ptrs);
   for (wb_ctx *c : b->inst) wb_destroy(c);
+  for (int k = 0; k < wb_batch::kMaxBranches; ++k) {
+    if (b->branch[k]) cudaStreamDestroy(b->branch[k]);
+    if (b->join[k]) cudaEventDestroy(b->join[k]);
+  }
+  if (b->fork) cudaEventDestroy(b->fork);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
   return WB_OK;
@@ -244,6 +266,11 @@ int wb_batch_create(const wb_config *cfgs, int32_t n, wb_batch **out) {
   }
   BCK(cudaSetDevice(b->device));
   BCK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+  BCK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+  for (int k = 0; k < wb_batch::kMaxBranches; ++k) {
+    BCK(cudaStreamCreateWithFlags(&b->branch[k], cudaStreamNonBlocking));
+    BCK(cudaEventCreateWithFlags(&b->join[k], cudaEventDisableTiming));
+  }
   for (int i = 0; i < n; ++i) {
     wb_config c = cfgs[i];
     b->pin_tx.push_back(c.tile_x > 0 ? c.tile_x : 0);

@@ -250,8 +250,8 @@ typedef struct wb_batch wb_batch;
 /* n independent instances (each its own grid, order, equilibrium, limiter), total-degree
  * basis, FP32-perturbation form, SSP-RK2, advanced together: per step one launch that
  * computes every instance's time step, then per RK stage one persistent launch per group
- * (instances of one degree on one tile shape) over a work list of cell tiles, the step
- * sequence replayed from a CUDA graph.  An instance's tile_x/tile_y/cells_per_thread pin
+ * (instances of one degree on one tile shape) over a work list of cell tiles, each group on
+ * its own branch of a CUDA graph that replays the step sequence.  An instance's tile_x/tile_y/cells_per_thread pin
  * its tile (32x8 or 16x16 at one cell per thread, 32x16 at two, 32x32 at four for degree
  * 0); 0 leaves it to the batch (32x8 until wb_batch_autotune). */
 int wb_batch_create(const wb_config *cfgs, int32_t n, wb_batch **out);
