@@ -42,7 +42,8 @@ struct wb_batch {
   std::vector<Group> groups;
   // Tile of each instance: pinned by its config, or the choice for its (degree, size class)
   std::vector<int> pin_tx, pin_ty, pin_cpt, size_class;
-  int choice[3][2][3] = {{{32, 8, 1}, {32, 8, 1}}, {{32, 8, 1}, {32, 8, 1}}, {{32, 8, 1}, {32, 8, 1}}};
+  // until wb_batch_autotune: the single grid's measured best per degree
+  int choice[3][2][3] = {{{32, 16, 2}, {32, 16, 2}}, {{32, 16, 2}, {32, 16, 2}}, {{32, 8, 1}, {32, 8, 1}}};
   int pos = 0;                        // some instance runs the positivity limiter
   StageArgs<float> *args = nullptr;  // [6 phases][2 stages][n]
   const float **state_ptrs = nullptr;  // [6 phases][n] current state per phase

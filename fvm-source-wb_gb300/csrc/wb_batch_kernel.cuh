@@ -113,9 +113,11 @@ __global__ void __launch_bounds__(256)
     const R *u = state[w.x];
     const int NQ = K + 1, NB = num_modes(K, 1);
     const Tab1D<R> &T = c_tab[K];
-    const int gi = w.y + tid % TX, gj = w.z + tid / TX;
+    // every cell of the item (a tile may hold more cells than the block has threads)
     double spx = 0.0, spy = 0.0;
-    if (gi < A.nx && gj < A.ny) {
+    for (int c = tid; c < TX * TY; c += blockDim.x) {
+      const int gi = w.y + c % TX, gj = w.z + c / TX;
+      if (gi >= A.nx || gj >= A.ny) continue;
       const long long cell = (long long)gj * A.pitch + gi;
       R rbar = R(0), pbar = R(0);
       for (int qa = 0; qa < NQ; ++qa)
@@ -130,12 +132,12 @@ __global__ void __launch_bounds__(256)
       R d2 = u[(long long)(2 * NB) * A.plane + cell], d3 = u[(long long)(3 * NB) * A.plane + cell];
       R r, p, sx, sy;
       mean_wave_speed(A, rbar, pbar, d0, d1, d2, d3, r, p, sx, sy);
-      spx = (double)sx;
-      spy = (double)sy;
-      if (!isfinite(spx) || !isfinite(spy)) {
+      if (!isfinite(sx) || !isfinite(sy)) {
         atomicOr(&A.dev->err, 1);
-        spx = spy = 0.0;
+        continue;
       }
+      spx = fmax(spx, (double)sx);
+      spy = fmax(spy, (double)sy);
     }
     double mx = block_max(spx, red, tid, blockDim.x);
     double my = block_max(spy, red, tid, blockDim.x);

@@ -759,8 +759,14 @@ int ctx_create(const wb_config *cfg, int row_align, wb_ctx **out) {
     ctx->TY = cfg->tile_y;
     ctx->CPT = cfg->cells_per_thread > 0 ? cfg->cells_per_thread : 1;
   } else if (is_fp32(ctx)) {
+    // untuned default: the measured best on large grids -- 32x8 at one cell per thread for
+    // degree 2, 32x16 at two cells per thread for degrees 0 and 1 (where compiled)
     ctx->TX = 32;
     ctx->TY = 8;
+    if (K <= 1 && tile_supported(1, K, cfg->basis, 32, 16, 2)) {
+      ctx->TY = 16;
+      ctx->CPT = 2;
+    }
   } else {
     ctx->TX = 16;
     ctx->TY = 8;

@@ -70,7 +70,9 @@ typedef struct {
                             positivity limiter (compute_positivity, :478-654) in delta form */
   int32_t precision;     /* WB_PREC_* */
   int32_t integrator;    /* WB_RK2 or WB_RK54 */
-  int32_t tile_x, tile_y;/* CTA tile in cells; 0 = tuned default */
+  int32_t tile_x, tile_y;/* CTA tile in cells; 0 = the tuned shape from the tile cache,
+                            else FP32 32x16 at two cells per thread for degrees 0 and 1
+                            (total-degree basis), 32x8 otherwise; FP64 16x8 */
   int32_t device;        /* CUDA device ordinal */
   int32_t riemann;       /* WB_RIEMANN_LLF or WB_RIEMANN_HLLC */
   int32_t cells_per_thread; /* cells each thread of the tile computes (the CTA has
@@ -253,7 +255,8 @@ typedef struct wb_batch wb_batch;
  * (instances of one degree on one tile shape) over a work list of cell tiles, each group on
  * its own branch of a CUDA graph that replays the step sequence.  An instance's tile_x/tile_y/cells_per_thread pin
  * its tile (32x8 or 16x16 at one cell per thread, 32x16 at two, 32x32 at four for degree
- * 0); 0 leaves it to the batch (32x8 until wb_batch_autotune). */
+ * 0); 0 leaves it to the batch (until wb_batch_autotune: 32x16 at two cells per thread for
+ * degrees 0 and 1, 32x8 for degree 2). */
 int wb_batch_create(const wb_config *cfgs, int32_t n, wb_batch **out);
 int wb_batch_destroy(wb_batch *b);
 const char *wb_batch_last_error(const wb_batch *b);
