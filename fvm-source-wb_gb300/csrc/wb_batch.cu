@@ -162,8 +162,14 @@ void make_items(const wb_batch *b, const std::vector<int> &sel, int ftx, int fty
         groups.back().TY != q.TY || groups.back().CPT != q.CPT)
       groups.push_back({q.K, q.TX, q.TY, q.CPT, (int)items.size(), 0, 0, 0});
     wb_batch::Group &g = groups.back();
-    for (int j0 = 0; j0 < c.ny; j0 += q.TY)
-      for (int i0 = 0; i0 < c.nx; i0 += q.TX) {
+    // row by row; within a row the columns rotated by the row index, so that a CTA's
+    // items it, it + G, ... do not keep to one tile column when G is a multiple of the row's
+    // tile count (the boundary columns, staged element by element, would fall to the same
+    // CTAs and make them stragglers)
+    const int ntx = (c.nx + q.TX - 1) / q.TX;
+    for (int r = 0, j0 = 0; j0 < c.ny; ++r, j0 += q.TY)
+      for (int k = 0; k < ntx; ++k) {
+        const int i0 = ((k + r) % ntx) * q.TX;
         items.push_back(make_int4(q.i, i0, j0, (q.K << 24) | (q.TX << 12) | q.TY));
         ++g.count;
       }

@@ -1435,20 +1435,31 @@ __global__ void __launch_bounds__(TX *TY / CPT, std::is_same<R, float>::value ? 
   // copies are issued right after it and tile_compute needs no closing barrier.
   const int G = gridDim.x;
   int t = blockIdx.x;
-  // tile coordinates of t and of t + G, stepped without a division per tile
-  const int gq = G / ntx, gr = G - (G / ntx) * ntx;
-  int cx = t % ntx, cy = t / ntx;  // tile t
-  auto advance = [&](int &x, int &y) {
-    x += gr;
-    y += gq;
-    if (x >= ntx) {
-      x -= ntx;
-      ++y;
-    }
+  // Tile t lies in row t / ntx; within a row the columns are taken in an order rotated by
+  // the row index, so that a CTA's tiles t, t + G, t + 2G, ... do not keep to one column when
+  // G is a multiple of ntx (the boundary columns, staged element by element, would then all
+  // fall to the same CTAs).  The CTAs still work on one compact band of rows at a time.
+  // The coordinates of t and of t + G are stepped without a division per tile.
+  struct Walk {
+    int px, cy, cys;  // t % ntx, t / ntx, (t / ntx) % ntx
   };
-  int nx_ = cx, ny_ = cy;  // tile t + G
-  advance(nx_, ny_);
-  if (t < ntiles) stage(cx * TX, cy * TY, 0);
+  const int gq = G / ntx, gr = G - (G / ntx) * ntx, gqm = gq % ntx;
+  auto advance = [&](Walk &w) {
+    w.px += gr;
+    w.cy += gq;
+    w.cys += gqm;
+    if (w.px >= ntx) {
+      w.px -= ntx;
+      ++w.cy;
+      ++w.cys;
+    }
+    if (w.cys >= ntx) w.cys -= ntx;
+  };
+  auto col = [&](const Walk &w) { return w.px + w.cys >= ntx ? w.px + w.cys - ntx : w.px + w.cys; };
+  Walk cur{t % ntx, t / ntx, (t / ntx) % ntx};  // tile t
+  Walk nxt = cur;                               // tile t + G
+  advance(nxt);
+  if (t < ntiles) stage(col(cur) * TX, cur.cy * TY, 0);
   cp_async_commit();
   for (int k = 0; t < ntiles; t += G, ++k) {
     const int b = k & 1;
@@ -1463,14 +1474,13 @@ __global__ void __launch_bounds__(TX *TY / CPT, std::is_same<R, float>::value ? 
       }
     }
     if (__syncthreads_or(!ok)) break;
-    if (t + G < ntiles) stage(nx_ * TX, ny_ * TY, b ^ 1);
+    if (t + G < ntiles) stage(col(nxt) * TX, nxt.cy * TY, b ^ 1);
     cp_async_commit();
     R *buf = bufs + b * L.buf;
-    tile_compute<R, K, BASIS, TX, TY, VAR, CPT>(A, lim, cx * TX, cy * TY, buf, flux, red, tid,
-                                                dt, speed, false);
-    cx = nx_;
-    cy = ny_;
-    advance(nx_, ny_);
+    tile_compute<R, K, BASIS, TX, TY, VAR, CPT>(A, lim, col(cur) * TX, cur.cy * TY, buf, flux,
+                                                red, tid, dt, speed, false);
+    cur = nxt;
+    advance(nxt);
   }
   __syncthreads();  // the last tile's readers are done before the reduction reuses `red`
   // wave-speed maxima of all this CTA's tiles: one block reduction per launch
