@@ -583,61 +583,69 @@ __device__ __forceinline__ bool tma_tile(const int use_tma, const int nx, const 
 // Issue the asynchronous copies that stage one tile (lower-left cell (i0, j0)) into `buf`:
 // the modes of the tile and a one-cell halo, the means of a two-cell halo when the
 // limiter is on, and the tile's equilibrium factors.  Boundary conditions are applied by
-// index mapping.  Warps copy whole rows (no per-element division).
+// index mapping.  The modes are staged by (row, chunk) slots: a thread keeps its slot and
+// walks the planes, so the slot's index arithmetic and boundary mapping are done once.
 template <typename R, int K, int BASIS, int TX, int TY, int NT = TX * TY>
 __device__ __forceinline__ void tile_load_async(const StageArgs<R> &A, const bool lim,
                                                 const int i0, const int j0, R *buf,
                                                 const int tid, const bool modes = true) {
   constexpr int nthr = NT;  // threads of the CTA
   const TileLayout L = tile_layout(K, BASIS, TX, TY, lim);
-  const int lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
   const int nx = A.nx, ny = A.ny, pitch = A.pitch;
   const long long P = A.plane;
-  constexpr int PX = TX + 8;
-  constexpr int VEC = 16 / (int)sizeof(R);  // elements per 16-byte chunk
-  constexpr int CPR = PX / VEC;             // chunks per stored row
-  // x-interior tile with 16-byte aligned rows: copy [i0-4, i0+TX+4) of every row in
-  // 16-byte chunks (rows still BC-mapped in y); otherwise element-wise with x mapping
-  const bool xin = i0 >= 4 && i0 + TX + 4 <= nx;
-  const bool vec = xin && (pitch % VEC) == 0;
-  // rows only 8-byte aligned (FP32, an even row pitch not a multiple of 4): 8-byte chunks
-  constexpr int VEC2 = 8 / (int)sizeof(R), CPR2 = PX / (VEC2 > 0 ? VEC2 : 1);
-  const bool vec2 = VEC2 == 2 && xin && (pitch % 2) == 0 && (P % 2) == 0;
-  const int nrow = NV * L.NB * L.RY;
-  if (!modes) {
-    // the modes come by TMA (k_stage)
-  } else if (vec) {
-    for (int k = tid; k < nrow * CPR; k += nthr) {
-      const int row = k / CPR, ch = k - row * CPR;
-      const int pl = row / L.RY, ry = row - pl * L.RY;
+  constexpr int PX = TX + 8, RY = TY + 2, RXY = PX * RY;
+  constexpr int NPL = NV * num_modes(K, BASIS);  // planes (variable x mode)
+  constexpr int VEC = 16 / (int)sizeof(R);       // elements per 16-byte chunk
+  constexpr int CPR = PX / VEC;                  // chunks per stored row
+  // Slot (ry, ch): stored row ry (grid row j0 + ry - 1, BC-mapped), chunk ch (grid columns
+  // c0 = i0 - 4 + ch * VEC .. c0 + VEC - 1) of every plane.  With at least as many threads
+  // as slots, PSTEP threads share a slot and take every PSTEP-th plane.
+  constexpr int NSLOT = RY * CPR;
+  constexpr bool WIDE = nthr >= NSLOT;
+  constexpr int PSTEP = WIDE ? nthr / NSLOT : 1;
+  // a chunk inside the grid is one 16-byte copy per plane (two 8-byte copies when FP32
+  // rows are only 8-byte aligned); a chunk reaching outside stages only the columns the
+  // tile reads, [i0 - xr, i0 + TX + xr) (the one-cell ring, two cells deep in x with the
+  // limiter), element by element with x mapping
+  const bool v16 = (pitch % VEC) == 0 && (P % VEC) == 0;
+  const bool v8 = !v16 && VEC == 4 && (pitch % 2) == 0 && (P % 2) == 0;
+  const int xr = L.lim ? 2 : 1;
+  if (modes) {
+    const int ps = WIDE ? tid / NSLOT : 0;  // the slot's first plane
+    for (int slot = WIDE ? (tid < PSTEP * NSLOT ? tid % NSLOT : NSLOT) : tid; slot < NSLOT;
+         slot += WIDE ? NSLOT : nthr) {
+      const int ry = slot / CPR, ch = slot - ry * CPR;
       const int gj = wrap_index(j0 + ry - 1, ny, A.bc_y);
-      cp_async<16>(buf + L.su + row * PX + ch * VEC,
-                   A.x + pl * P + (long long)gj * pitch + (i0 - 4) + ch * VEC);
-    }
-  } else if (vec2) {
-    for (int k = tid; k < nrow * CPR2; k += nthr) {
-      const int row = k / CPR2, ch = k - row * CPR2;
-      const int pl = row / L.RY, ry = row - pl * L.RY;
-      const int gj = wrap_index(j0 + ry - 1, ny, A.bc_y);
-      cp_async<8>(buf + L.su + row * PX + ch * 2,
-                  A.x + pl * P + (long long)gj * pitch + (i0 - 4) + ch * 2);
-    }
-  } else {
-    // element-wise with x mapping: the one-cell ring, two cells deep in x with the limiter
-    // (the chunked copies above always cover columns i0 - 4 .. i0 + TX + 3)
-    const int xr = L.lim ? 2 : 1;
-    int gc[3];
+      const int c0 = i0 - 4 + ch * VEC;
+      const R *src = A.x + (long long)ps * P + (long long)gj * pitch;
+      R *dst = buf + L.su + ps * RXY + ry * PX + ch * VEC;
+      const long long sstep = PSTEP * P;
+      if (c0 >= 0 && c0 + VEC <= nx && (v16 || v8)) {
+        src += c0;
+        if (v16) {
+#pragma unroll 4
+          for (int pl = ps; pl < NPL; pl += PSTEP, src += sstep, dst += PSTEP * RXY)
+            cp_async<16>(dst, src);
+        } else {
+#pragma unroll 4
+          for (int pl = ps; pl < NPL; pl += PSTEP, src += sstep, dst += PSTEP * RXY) {
+            cp_async<8>(dst, src);
+            cp_async<8>(dst + 2, src + 2);
+          }
+        }
+      } else {
+        const int lo = max(c0, i0 - xr), hi = min(c0 + VEC, i0 + TX + xr);
+        if (lo < hi) {
+          int gi[VEC];
 #pragma unroll
-    for (int k = 0; k < 3; ++k) gc[k] = wrap_index(i0 + lane + 32 * k - xr, nx, A.bc_x);
-    for (int row = warp; row < nrow; row += nwarp) {
-      const int pl = row / L.RY, ry = row - pl * L.RY;
-      const int gj = wrap_index(j0 + ry - 1, ny, A.bc_y);
-      const R *src = A.x + pl * P + (long long)gj * pitch;
-      R *dst = buf + L.su + row * PX + 4 - xr;
+          for (int e = 0; e < VEC; ++e) gi[e] = lo + e < hi ? wrap_index(lo + e, nx, A.bc_x) : 0;
+          dst += lo - c0;
+          for (int pl = ps; pl < NPL; pl += PSTEP, src += sstep, dst += PSTEP * RXY) {
 #pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        const int c = lane + 32 * k;
-        if (c < TX + 2 * xr) cp_async<sizeof(R)>(dst + c, src + gc[k]);
+            for (int e = 0; e < VEC; ++e)
+              if (lo + e < hi) cp_async<sizeof(R)>(dst + e, src + gi[e]);
+          }
+        }
       }
     }
   }

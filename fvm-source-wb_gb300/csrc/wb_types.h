@@ -143,8 +143,6 @@ __host__ __device__ inline TileLayout tile_layout(int K, int basis, int TX, int 
   L.buf = (L.eq + neq + 31) & ~31;  // 128-byte aligned double buffers (TMA destinations)
   return L;
 }
-// Largest tile width the staging code handles (three 32-wide chunks of a halo row).
-constexpr int TILE_X_MAX = 92;
 
 // Shared-memory bytes of the stage kernel for a TX x TY tile: reduction scratch, two
 // staged tiles, and the x/y face fluxes of one tile.
