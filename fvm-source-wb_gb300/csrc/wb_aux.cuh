@@ -43,7 +43,7 @@ __global__ void k_limit(const __grid_constant__ StageArgs<R> A, R *u) {
     R dl[NV * NB];
 #pragma unroll
     for (int k = 0; k < NV * NB; ++k) dl[k] = u[(long long)k * P + cell];
-    positivity_cell<R, K, BASIS>(A, dl, fx, fy);
+    positivity_cell<R, K, BASIS>(A, A.eq_kind, dl, fx, fy);
 #pragma unroll
     for (int k = 1; k < NV * NB; ++k)
       if (k % NB) u[(long long)k * P + cell] = dl[k];
@@ -57,7 +57,7 @@ __global__ void k_limit(const __grid_constant__ StageArgs<R> A, R *u) {
 #pragma unroll
     for (int m = 0; m < NB; ++m) w[m] = u[(long long)(v * NB + m) * P + cell];
     const R *m0 = u + (long long)(v * NB) * P;
-    limit_modes<R, K, BASIS>(A, w, 1, w[0], m0[gj * nx + iw], m0[gj * nx + ie], m0[js * nx + gi],
+    limit_modes<R, K, BASIS>(A, A, w, 1, w[0], m0[gj * nx + iw], m0[gj * nx + ie], m0[js * nx + gi],
                              m0[jn * nx + gi]);
 #pragma unroll
     for (int m = 1; m < NB; ++m) u[(long long)(v * NB + m) * P + cell] = w[m];

@@ -33,19 +33,25 @@ struct wb_batch {
   int4 *items = nullptr;  // all items, one contiguous range per group
   int nitems = 0;
   size_t items_cap = 0;
-  // A group = the items of one degree K on one tile shape (and cells per thread),
-  // launched by its own kernel.
+  // A group = the items of one degree K on one tile shape (and cells per thread) whose
+  // instances share their physical constants, launched by its own kernel; rep is one of
+  // its instances, whose stage arguments carry the group's constants to the launch.
   struct Group {
     int K, TX, TY, CPT, off, count, buf;
     size_t smem;
+    int rep;
   };
   std::vector<Group> groups;
+  // physics class of each instance: the first instance with the same physical constants,
+  // boundary conditions and limiter (what the stage kernel takes from its launch constants)
+  std::vector<int> phys;
   // Tile of each instance: pinned by its config, or the choice for its (degree, size class)
   std::vector<int> pin_tx, pin_ty, pin_cpt, size_class;
   // until wb_batch_autotune: the single grid's measured best per degree
   int choice[3][2][3] = {{{32, 16, 2}, {32, 16, 2}}, {{32, 16, 2}, {32, 16, 2}}, {{32, 8, 1}, {32, 8, 1}}};
   int pos = 0;                        // some instance runs the positivity limiter
   StageArgs<float> *args = nullptr;  // [6 phases][2 stages][n]
+  std::vector<StageArgs<float>> hargs;  // host copy of args (the groups' launch constants)
   const float **state_ptrs = nullptr;  // [6 phases][n] current state per phase
   int phase = 0;
   int dt_mode = -1;
@@ -82,6 +88,7 @@ int build_args(wb_batch *b, int dt_mode, double dt) {
       sp[(size_t)p * n + i] = two[0].x;
     }
   BCK(cudaMemcpyAsync(b->args, h.data(), h.size() * sizeof(StageArgs<float>), cudaMemcpyHostToDevice, b->stream));
+  b->hargs = h;
   BCK(cudaMemcpyAsync(b->state_ptrs, sp.data(), sp.size() * sizeof(float *), cudaMemcpyHostToDevice, b->stream));
   BCK(cudaStreamSynchronize(b->stream));
   b->dt_mode = dt_mode;
@@ -109,7 +116,8 @@ int launch_phase(wb_batch *b, int p) {
     const wb_batch::Group &g = b->groups[gi];
     cudaStream_t s = b->branch[std::min((int)gi, nb - 1)];
     for (int st = 0; st < 2; ++st)
-      BCK(launch_batch_stage(b->args + ((size_t)p * 2 + st) * n, b->items + g.off, g.count, g.buf,
+      BCK(launch_batch_stage(b->hargs[((size_t)p * 2 + st) * n + g.rep],
+                             b->args + ((size_t)p * 2 + st) * n, b->items + g.off, g.count, g.buf,
                              g.smem, b->pos, g.K, g.TX, g.TY, g.CPT, &grid, s));
   }
   for (int k = 0; k < nb; ++k) {
@@ -117,6 +125,18 @@ int launch_phase(wb_batch *b, int p) {
     BCK(cudaStreamWaitEvent(b->stream, b->join[k], 0));
   }
   return WB_OK;
+}
+
+// Whether two instances' stage arguments agree in everything the stage kernel takes from
+// its launch constants rather than from the instance (tile_compute's A): physical
+// constants, boundary conditions, limiter and flux options.
+bool same_launch_constants(const StageArgs<float> &a, const StageArgs<float> &c) {
+  return a.bc_x == c.bc_x && a.bc_y == c.bc_y && a.llf_speed == c.llf_speed &&
+         a.limiter == c.limiter && a.lim_y == c.lim_y && a.riemann == c.riemann &&
+         a.gamma == c.gamma && a.gm1 == c.gm1 && a.igm1 == c.igm1 && a.hgam == c.hgam &&
+         a.gx == c.gx && a.gy == c.gy && a.rho0 == c.rho0 && a.p0 == c.p0 &&
+         a.kpoly == c.kpoly && a.npoly == c.npoly && a.lim_norm == c.lim_norm &&
+         a.lim_tol == c.lim_tol && a.pos_eps == c.pos_eps;
 }
 
 // Size class of an instance for the tile choice: small grids (side < 128) and the rest.
@@ -140,27 +160,31 @@ void instance_tile(const wb_batch *b, int i, int *tx, int *ty, int *cpt) {
 void make_items(const wb_batch *b, const std::vector<int> &sel, int ftx, int fty, int fcpt,
                 std::vector<int4> &items, std::vector<wb_batch::Group> &groups) {
   struct Key {
-    int K, TX, TY, CPT, i;
+    int K, TX, TY, CPT, cls, i;
   };
   std::vector<Key> keys;
   for (int i : sel) {
     int tx = ftx, ty = fty, cpt = fcpt;
     if (tx <= 0) instance_tile(b, i, &tx, &ty, &cpt);
-    keys.push_back({b->cfgs[i].order, tx, ty, cpt, i});
+    keys.push_back({b->cfgs[i].order, tx, ty, cpt, b->phys[i], i});
   }
-  // degree 2 first (the costliest launches start first), then by tile shape
+  // degree 2 first (the costliest launches start first), then by tile shape and physics
   std::stable_sort(keys.begin(), keys.end(), [](const Key &x, const Key &y) {
     if (x.K != y.K) return x.K > y.K;
     if (x.TX != y.TX) return x.TX > y.TX;
     if (x.TY != y.TY) return x.TY < y.TY;
-    return x.CPT < y.CPT;
+    if (x.CPT != y.CPT) return x.CPT < y.CPT;
+    return x.cls < y.cls;
   });
+  int cls = -1;
   for (size_t k = 0; k < keys.size(); ++k) {
     const Key &q = keys[k];
     const wb_config &c = b->cfgs[q.i];
     if (groups.empty() || groups.back().K != q.K || groups.back().TX != q.TX ||
-        groups.back().TY != q.TY || groups.back().CPT != q.CPT)
-      groups.push_back({q.K, q.TX, q.TY, q.CPT, (int)items.size(), 0, 0, 0});
+        groups.back().TY != q.TY || groups.back().CPT != q.CPT || cls != q.cls) {
+      groups.push_back({q.K, q.TX, q.TY, q.CPT, (int)items.size(), 0, 0, 0, q.i});
+      cls = q.cls;
+    }
     wb_batch::Group &g = groups.back();
     // row by row; within a row the columns rotated by the row index, so that a CTA's
     // items it, it + G, ... do not keep to one tile column when G is a multiple of the row's
@@ -300,6 +324,15 @@ int wb_batch_create(const wb_config *cfgs, int32_t n, wb_batch **out) {
     b->inst.push_back(ctx);
     b->cfgs.push_back(c);
     if (c.limiter == 2 && c.order >= 1) b->pos = 1;
+    // physics class: compared on the stage arguments the kernel takes as launch constants
+    StageArgs<float> ai[2], aj[2];
+    if ((rc = ctx_rk2_stage_args(ctx, 0, 1, 0.0, ai))) return berr(b, rc, "instance arguments");
+    int cls = i;
+    for (int j = 0; j < i && cls == i; ++j)
+      if (b->phys[j] == j && !ctx_rk2_stage_args(b->inst[j], 0, 1, 0.0, aj) &&
+          same_launch_constants(ai[0], aj[0]))
+        cls = j;
+    b->phys.push_back(cls);
   }
   int rc = build_worklist(b);
   if (rc) return rc;
@@ -403,7 +436,8 @@ int wb_batch_autotune(wb_batch *b, int32_t reps, int32_t *tiles) {
         for (int r = 0; r <= reps && !rc; ++r) {  // launch 0 warms up
           if (r == 1 && cudaEventRecord(e0, b->stream) != cudaSuccess) rc = WB_ERR_CUDA;
           for (const wb_batch::Group &g : groups)
-            if (!rc && launch_batch_stage(a1, b->items + g.off, g.count, g.buf, g.smem, b->pos,
+            if (!rc && launch_batch_stage(b->hargs[((size_t)b->phase * 2 + 0) * n + g.rep], a1,
+                                          b->items + g.off, g.count, g.buf, g.smem, b->pos,
                                           g.K, g.TX, g.TY, g.CPT, nullptr, b->stream) != cudaSuccess)
               rc = berr(b, WB_ERR_CUDA, "autotune launch failed");
         }

@@ -28,7 +28,7 @@ __device__ __forceinline__ void item_load(const StageArgs<R> *__restrict__ args,
   // the instance's time step (k_batch_begin_step computed it once per step), staged with
   // the tile
   if (tid == 0) cp_async<8>(&sdt, &A.dev->dt[A.parity]);
-  const bool lim = A.limiter == 1 && A.lim_y && K >= 1;
+  const bool lim = A.limiter == 1 && A.lim_y && K >= 1;  // the same for the whole group
   tile_load_async<R, K, 1, TX, TY, NT>(A, lim, w.y, w.z, buf, tid);
 }
 
@@ -37,14 +37,19 @@ __device__ __forceinline__ void item_load(const StageArgs<R> *__restrict__ args,
 __host__ __device__ constexpr int batch_min_blocks(int K) { return K == 0 ? 4 : K == 1 ? 3 : 2; }
 
 // Persistent batched stage for the items of one group (degree K, TX x TY tiles, CPT cells
-// per thread): CTAs stride over the group's work list; the next item is staged (cp.async)
-// while the current one is computed.  bufsz = the largest tile buffer of the group.  One
-// kernel per degree gives each its own register budget (and occupancy) and no runtime
-// dispatch on K.
+// per thread, one set of physical constants): CTAs stride over the group's work list; the
+// next item is staged (cp.async) while the current one is computed.  bufsz = the largest
+// tile buffer of the group.  One kernel per degree gives each its own register budget (and
+// occupancy) and no runtime dispatch on K.  Q: the stage arguments of one instance of the
+// group, whose physical constants, boundary conditions, limiter and stage flags every
+// instance of the group shares; as a kernel parameter they are free operands of the
+// arithmetic (from shared memory they cost a load each and registers to hold them).  The
+// item's own arguments (grid, buffers, spacing, equilibrium kind, run state) come from
+// `args`, staged into shared memory with the tile.
 template <typename R, int K, int TX, int TY, bool POS, int CPT>
 __global__ void __launch_bounds__(TX * TY / CPT, batch_min_blocks(K))
-    k_batch_stage(const StageArgs<R> *__restrict__ args, const int4 *__restrict__ items, int nitems,
-                  int bufsz) {
+    k_batch_stage(const __grid_constant__ StageArgs<R> Q, const StageArgs<R> *__restrict__ args,
+                  const int4 *__restrict__ items, int nitems, int bufsz) {
   constexpr int NT = TX * TY / CPT;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ __align__(16) StageArgs<R> sA[2];  // instance arguments of the staged items
@@ -67,12 +72,12 @@ __global__ void __launch_bounds__(TX * TY / CPT, batch_min_blocks(K))
                                   bufs + ((k + 1) & 1) * bufsz, tid);
     cp_async_commit();
     const int4 w = items[it];
-    const StageArgs<R> &A = sA[k & 1];
+    const StageArgs<R> &I = sA[k & 1];
     R *buf = bufs + (k & 1) * bufsz;
     const double dt = sdt[k & 1];
-    const bool lim = A.limiter == 1 && A.lim_y && K >= 1;
+    const bool lim = Q.limiter == 1 && Q.lim_y && K >= 1;
     tile_compute<R, K, 1, TX, TY, POS ? WB_VAR_POSITIVITY : 0, CPT>(
-        A, lim, w.y, w.z, buf, flux, red, tid, dt, nullptr, false, true);
+        Q, I, lim, w.y, w.z, buf, flux, red, tid, dt, nullptr, false, true);
   }
   cp_async_wait<0>();
 }

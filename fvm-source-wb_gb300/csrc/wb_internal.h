@@ -57,10 +57,11 @@ cudaError_t launch_f64_to_f32(float *out, const double *in, long long n, cudaStr
 // device-to-device copy on the SMs (16-byte aligned buffers, a multiple of 16 bytes)
 cudaError_t launch_copy_device(void *out, const void *in, size_t bytes, cudaStream_t s);
 
-// batched form (FP32): persistent stage over a work list; per-instance max speed
-cudaError_t launch_batch_stage(const StageArgs<float> *args, const int4 *items, int nitems,
-                               int bufsz, size_t smem, int pos, int K, int TX, int TY, int CPT,
-                               int *grid_out, cudaStream_t s);
+// batched form (FP32): persistent stage over a work list (Q: the group's shared constants,
+// args: every instance's arguments); per-instance max speed
+cudaError_t launch_batch_stage(const StageArgs<float> &Q, const StageArgs<float> *args,
+                               const int4 *items, int nitems, int bufsz, size_t smem, int pos,
+                               int K, int TX, int TY, int CPT, int *grid_out, cudaStream_t s);
 // the tile shapes (TX, TY, cells per thread) the batch kernels compile for degree K
 bool batch_tile_supported(int order, int tx, int ty, int cpt);
 int batch_tile_candidates(int order, int (*out)[3], int max);

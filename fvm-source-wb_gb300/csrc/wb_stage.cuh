@@ -92,13 +92,15 @@ __device__ __forceinline__ float eq_pow(float s, float n) { return __powf(s, n);
 __device__ __forceinline__ double eq_pow(double s, double n) { return pow(s, n); }
 
 // Equilibrium density/pressure from the separable factors (see wb_tables.cpp).
+// kind: the instance's equilibrium (its eq_kind); the constants come from A.
 template <typename R>
-__device__ __forceinline__ void eq_point(const StageArgs<R> &A, R fx, R fy, R &re, R &pe) {
-  if (A.eq_kind == 1) {
+__device__ __forceinline__ void eq_point(const StageArgs<R> &A, const int kind, R fx, R fy, R &re,
+                                         R &pe) {
+  if (kind == 1) {
     R t = fx * fy;
     re = A.rho0 * t;
     pe = A.p0 * t;
-  } else if (A.eq_kind == 2) {
+  } else if (kind == 2) {
     R s = fx + fy;
     re = eq_pow(s, A.npoly);
     pe = A.kpoly * (re * s);
@@ -106,6 +108,10 @@ __device__ __forceinline__ void eq_point(const StageArgs<R> &A, R fx, R fy, R &r
     re = R(0);
     pe = R(0);
   }
+}
+template <typename R>
+__device__ __forceinline__ void eq_point(const StageArgs<R> &A, R fx, R fy, R &re, R &pe) {
+  eq_point(A, A.eq_kind, fx, fy, re, pe);
 }
 
 // CFL wave speeds |u| + c and |v| + c of a cell from its mean perturbation d0..d3 and its
@@ -352,14 +358,15 @@ __device__ __forceinline__ void face_point_pk(const StageArgs<float> &A, const f
 
 // Limit one cell's modes in place (base[m*mstride] is mode m of one variable).
 template <typename R, int K, int BASIS>
-__device__ __forceinline__ void limit_modes(const StageArgs<R> &A, R *base, int mstride, R m0,
+__device__ __forceinline__ void limit_modes(const StageArgs<R> &A, const StageArgs<R> &I,
+                                            R *base, int mstride, R m0,
                                             R mw, R me, R ms, R mn) {
   if constexpr (K >= 1) {
     constexpr int NB = num_modes(K, BASIS);
     constexpr int M10 = mode_index(K, BASIS, 1, 0), M01 = mode_index(K, BASIS, 0, 1);
     R sx = base[M10 * mstride], sy = base[M01 * mstride];
-    R l1 = gminmod(A.lim_norm * sx, me - m0, m0 - mw, A.lim_Mdx2) / A.lim_norm;
-    R l2 = gminmod(A.lim_norm * sy, mn - m0, m0 - ms, A.lim_Mdy2) / A.lim_norm;
+    R l1 = gminmod(A.lim_norm * sx, me - m0, m0 - mw, I.lim_Mdx2) / A.lim_norm;
+    R l2 = gminmod(A.lim_norm * sy, mn - m0, m0 - ms, I.lim_Mdy2) / A.lim_norm;
     if (fabs(l1 - sx) > A.lim_tol || fabs(l2 - sy) > A.lim_tol) {
       base[M10 * mstride] = l1;
       base[M01 * mstride] = l2;
@@ -381,8 +388,8 @@ __device__ __forceinline__ void limit_modes(const StageArgs<R> &A, R *base, int 
 // (theta = t = 1) is not written.  Not inlined: it is off the default path, and its
 // point loops stay rolled to keep the stage kernels small.
 template <typename R, int K, int BASIS>
-__device__ __noinline__ void positivity_cell(const StageArgs<R> &A, R *d, const R *fx,
-                                             const R *fy) {
+__device__ __noinline__ void positivity_cell(const StageArgs<R> &A, const int kind, R *d,
+                                             const R *fx, const R *fy) {
   if constexpr (K >= 1) {
     constexpr int NB = num_modes(K, BASIS), NQ = K + 1;
     using T = TC<R, K>;
@@ -395,7 +402,7 @@ __device__ __noinline__ void positivity_cell(const StageArgs<R> &A, R *d, const 
 #pragma unroll 1
       for (int qb = 0; qb < NQ; ++qb) {
         R re, pe;
-        eq_point(A, fx[qa], fy[qb], re, pe);
+        eq_point(A, kind, fx[qa], fy[qb], re, pe);
         pe *= A.igm1;
         const R w = R(0.25) * T::wq(qa) * T::wq(qb);
 #pragma unroll
@@ -689,8 +696,13 @@ __device__ __forceinline__ void tile_load_async(const StageArgs<R> &A, const boo
 // With end_sync it ends with a CTA barrier, after which `buf` and the flux area may be
 // reused.  The wave speed goes to speed_acc (the caller reduces later), or by warp atomics
 // (warp_speed), or by a CTA reduction and one atomic.
+// A holds the launch's constants (physics, boundary conditions, limiter, RK stage flags);
+// I the instance: its grid, buffers, spacing, equilibrium kind and run state.  A single
+// grid passes its arguments as both; the batched form passes the group's constants as A
+// (kernel parameters: free operands) and the item's instance as I.
 template <typename R, int K, int BASIS, int TX, int TY, int VAR, int CPT = 1>
-__device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool lim_,
+__device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const StageArgs<R> &I,
+                                             const bool lim_,
                                              const int i0, const int j0, R *buf, R *flux,
                                              double *red, const int tid, const double dt,
                                              R *speed_acc = nullptr,
@@ -710,9 +722,10 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
   static_assert((TX * TY) % (32 * CPT) == 0, "whole warps of CPT cells per thread");
   constexpr int nthr = TX * TY / CPT;  // threads of the CTA
   constexpr int NCELL = TX * TY;
-  const int nx = A.nx, ny = A.ny, pitch = A.pitch;
-  const long long P = A.plane;
+  const int nx = I.nx, ny = I.ny, pitch = I.pitch;
+  const long long P = I.plane;
   const bool lim = lim_;
+  const int eqk = I.eq_kind;
   R *su = buf + L.su + 3;
   const R *sm = buf + L.sm + 3;  // [NV][2][RX]: means of rows j0 - 2 and j0 + TY + 1
   // volume-point factors are indexed from the tile's first column / row (halo at -1)
@@ -736,7 +749,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
       const R *sd = sm + v * 2 * RX + rx;
       const R ms = ry > 0 ? mp[-RX] : sd[0];
       const R mn = ry < RY - 1 ? mp[RX] : sd[RX];
-      limit_modes<R, K, BASIS>(A, su + (v * NB) * RXY + ry * RX + rx, RXY, mp[0], mp[-1], mp[1],
+      limit_modes<R, K, BASIS>(A, I, su + (v * NB) * RXY + ry * RX + rx, RXY, mp[0], mp[-1], mp[1],
                                ms, mn);
     }
     __syncthreads();
@@ -747,7 +760,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
       R dl[NV * NB];
 #pragma unroll
       for (int k = 0; k < NV * NB; ++k) dl[k] = base[k * RXY];
-      positivity_cell<R, K, BASIS>(A, dl, sfxv + (rx - 1) * NQ, sfyv + (ry - 1) * NQ);
+      positivity_cell<R, K, BASIS>(A, eqk, dl, sfxv + (rx - 1) * NQ, sfyv + (ry - 1) * NQ);
 #pragma unroll
       for (int k = 0; k < NV * NB; ++k) base[k * RXY] = dl[k];
     }
@@ -798,7 +811,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
             s2 = __ffma2_rn(clr[v][b], make_float2(T::B(b, q), T::B(b, q)), s2);
           d2[v] = s2;
         }
-        eq_point(A, fxf, sfyv[fj * NQ + q], re, pe);
+        eq_point(A, eqk, fxf, sfyv[fj * NQ + q], re, pe);
         face_point_pk<0>(A, d2, re, pe, F);
         const float2 Fp[2] = {make_float2(F[0], F[1]), make_float2(F[2], F[3])};
 #pragma unroll
@@ -809,7 +822,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
             mom[pp][c] = __ffma2_rn(Fp[pp], make_float2(w, w), q == 0 ? make_float2(0.f, 0.f) : mom[pp][c]);
           }
       }
-      const float2 h2 = make_float2(A.hidx, A.hidx);
+      const float2 h2 = make_float2(I.hidx, I.hidx);
 #pragma unroll
       for (int pp = 0; pp < 2; ++pp)
 #pragma unroll
@@ -854,7 +867,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
         dL[v] = sl;
         dR[v] = sr;
       }
-      eq_point(A, fxf, sfyv[fj * NQ + q], re, pe);
+      eq_point(A, eqk, fxf, sfyv[fj * NQ + q], re, pe);
       face_point<R, 0, HLLC>(A, dL, dR, re, pe, F);
 #pragma unroll
       for (int v = 0; v < NV; ++v)
@@ -865,7 +878,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
 #pragma unroll
     for (int v = 0; v < NV; ++v)
 #pragma unroll
-      for (int b = 0; b < NQ; ++b) sfx[(v * NQ + b) * FXS + f] = mom[v][b] * A.hidx;
+      for (int b = 0; b < NQ; ++b) sfx[(v * NQ + b) * FXS + f] = mom[v][b] * I.hidx;
     }
     } else {
     const int f = fa - FXP;
@@ -904,7 +917,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
             s2 = __ffma2_rn(cbt[v][a], make_float2(T::B(a, q), T::B(a, q)), s2);
           d2[v] = s2;
         }
-        eq_point(A, sfxv[fi * NQ + q], fyf, re, pe);
+        eq_point(A, eqk, sfxv[fi * NQ + q], fyf, re, pe);
         face_point_pk<1>(A, d2, re, pe, F);
         const float2 Fp[2] = {make_float2(F[0], F[1]), make_float2(F[2], F[3])};
 #pragma unroll
@@ -915,7 +928,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
             mom[pp][c] = __ffma2_rn(Fp[pp], make_float2(w, w), q == 0 ? make_float2(0.f, 0.f) : mom[pp][c]);
           }
       }
-      const float2 h2 = make_float2(A.hidy, A.hidy);
+      const float2 h2 = make_float2(I.hidy, I.hidy);
 #pragma unroll
       for (int pp = 0; pp < 2; ++pp)
 #pragma unroll
@@ -958,7 +971,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
         dB[v] = sb;
         dT[v] = st;
       }
-      eq_point(A, sfxv[fi * NQ + q], fyf, re, pe);
+      eq_point(A, eqk, sfxv[fi * NQ + q], fyf, re, pe);
       face_point<R, 1, HLLC>(A, dB, dT, re, pe, F);
 #pragma unroll
       for (int v = 0; v < NV; ++v)
@@ -968,7 +981,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
 #pragma unroll
     for (int v = 0; v < NV; ++v)
 #pragma unroll
-      for (int a = 0; a < NQ; ++a) sfy[(v * NQ + a) * FYS + f] = mom[v][a] * A.hidy;
+      for (int a = 0; a < NQ; ++a) sfy[(v * NQ + a) * FYS + f] = mom[v][a] * I.hidy;
     }
     }
   }
@@ -999,7 +1012,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
   // thread's later cells.)
   constexpr bool UN = CPT == 1 && !FP64 &&
                       NV * NB * TX * TY <= NV * NQ * (TY * (TX + 1) + (TY + 1) * TX);
-  const bool un = UN && A.o[0].out != nullptr && A.o[0].in[0] != nullptr;
+  const bool un = UN && I.o[0].out != nullptr && I.o[0].in[0] != nullptr;
   R *sun = flux;  // [NV*NB][TX*TY]
   // With the minmod limiter on that input (SSP-RK2's U^n), the means of its one-cell ring
   // are staged behind it, [NV][W: TY, E: TY, S: TX, N: TX], so the limiter of U^n reads
@@ -1009,7 +1022,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
   constexpr bool UNL = UN && K >= 1 &&
                        NV * NB * TX * TY + NV * RING <= NV * NQ * (TY * (TX + 1) + (TY + 1) * TX);
   const bool full = i0 + TX <= nx && j0 + TY <= ny;
-  const bool unl = UNL && un && full && A.o[0].lim[0] && A.limiter == 1;
+  const bool unl = UNL && un && full && I.o[0].lim[0] && A.limiter == 1;
   R *sring = sun + NV * NB * NCELL;
   auto source_edges = [&]() {
     if constexpr (!FP64) {
@@ -1059,7 +1072,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
   if (un) {
     if (active) source_edges();
     __syncthreads();  // every thread is done with the face fluxes
-    const R *in0 = A.o[0].in[0];
+    const R *in0 = I.o[0].in[0];
     if (full && (pitch % 4) == 0) {
       // 16-byte chunks: a thread keeps its (row, chunk) and walks the planes
       constexpr int CPR_U = TX / 4, PCH = TY * CPR_U, NCH = NV * NB * PCH;
@@ -1144,7 +1157,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
             dm = __ffma2_rn(cmm[b], B2, dm);
           }
           float re, pe;
-          eq_point(A, fx, sfyv[ty * NQ + qb], re, pe);
+          eq_point(A, eqk, fx, sfyv[ty * NQ + qb], re, pe);
           if (A.compute_speed) {
             float ww = 0.25f * T::wq(qa) * T::wq(qb);
             rbar += re * ww;
@@ -1178,8 +1191,8 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
         float dwx[NQ], bwy[NQ];
 #pragma unroll
         for (int a = 0; a < NQ; ++a) {
-          dwx[a] = A.hidx * T::DW(a, qa);
-          bwy[a] = A.hidy * T::BW(a, qa);
+          dwx[a] = I.hidx * T::DW(a, qa);
+          bwy[a] = I.hidy * T::BW(a, qa);
         }
 #pragma unroll
         for (int v = 0; v < NV; ++v)
@@ -1225,7 +1238,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
           for (int b = 0; b < NQ; ++b) s += c[v][b] * T::B(b, qb);
           d[v] = s;
         }
-        eq_point(A, fx, sfyv[ty * NQ + qb], re, pe);
+        eq_point(A, eqk, fx, sfyv[ty * NQ + qb], re, pe);
         if (A.compute_speed) {
           R ww = R(0.25) * T::wq(qa) * T::wq(qb);
           rbar += re * ww;
@@ -1235,7 +1248,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
         // x fluxes are weighted by 0.5/dx once per qa below; y fluxes take 0.5/dy here
 #pragma unroll
         for (int b = 0; b < NQ; ++b) {
-          const R dwy = b > 0 ? A.hidy * T::DW(b, qb) : R(0);
+          const R dwy = b > 0 ? I.hidy * T::DW(b, qb) : R(0);
 #pragma unroll
           for (int v = 0; v < NV; ++v) {
             if (BASIS == 0 || b < K) Pq[v][b] += Fx[v] * T::BW(b, qb);
@@ -1246,7 +1259,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
       }
       R dwx[NQ];
 #pragma unroll
-      for (int a = 0; a < NQ; ++a) dwx[a] = A.hidx * T::DW(a, qa);
+      for (int a = 0; a < NQ; ++a) dwx[a] = I.hidx * T::DW(a, qa);
 #pragma unroll
       for (int v = 0; v < NV; ++v)
 #pragma unroll
@@ -1272,7 +1285,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
     const long long cell = (long long)gj * pitch + gi;
 #pragma unroll
     for (int oi = 0; oi < 2; ++oi) {
-      const Combo<R> &o = A.o[oi];
+      const Combo<R> &o = I.o[oi];
       if (o.out == nullptr) continue;
       R val[NV][NB];
       const R cdt = o.cdt * (R)dt;
@@ -1302,7 +1315,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
           for (int v = 0; v < NV; ++v)
 #pragma unroll
             for (int m = 0; m < NB; ++m) dl[v * NB + m] = w[v][m];
-          positivity_cell<R, K, BASIS>(A, dl, sfxv + tx * NQ, sfyv + ty * NQ);
+          positivity_cell<R, K, BASIS>(A, eqk, dl, sfxv + tx * NQ, sfyv + ty * NQ);
 #pragma unroll
           for (int v = 0; v < NV; ++v)
 #pragma unroll
@@ -1317,7 +1330,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
             const R me = tx < TX - 1 ? m0[1] : rg[TY + ty];
             const R ms = ty > 0 ? m0[-TX] : rg[2 * TY + tx];
             const R mn = ty < TY - 1 ? m0[TX] : rg[2 * TY + TX + tx];
-            limit_modes<R, K, BASIS>(A, &w[v][0], 1, w[v][0], mw, me, ms, mn);
+            limit_modes<R, K, BASIS>(A, I, &w[v][0], 1, w[v][0], mw, me, ms, mn);
           }
         } else if (o.lim[ii] && A.limiter == 1 && K >= 1) {
           int iw = wrap_index(gi - 1, nx, A.bc_x), ie = wrap_index(gi + 1, nx, A.bc_x);
@@ -1325,7 +1338,7 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
 #pragma unroll
           for (int v = 0; v < NV; ++v) {
             const R *m0p = in + (long long)(v * NB) * P;
-            limit_modes<R, K, BASIS>(A, &w[v][0], 1, w[v][0], m0p[(long long)gj * pitch + iw],
+            limit_modes<R, K, BASIS>(A, I, &w[v][0], 1, w[v][0], m0p[(long long)gj * pitch + iw],
                                      m0p[(long long)gj * pitch + ie],
                                      m0p[(long long)js * pitch + gi],
                                      m0p[(long long)jn * pitch + gi]);
@@ -1350,8 +1363,8 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
         R r, p, cx, cy;
         mean_wave_speed(A, rbar, pbar, val[0][0], val[1][0], val[2][0], val[3][0], r, p, cx, cy);
         bool bad = !(r > R(0)) || !(p > R(0)) || !isfinite(cx) || !isfinite(cy);
-        if (A.eq_kind == 0) bad = !isfinite(cx) || !isfinite(cy);
-        if (bad) atomicOr(&A.dev->err, 1);
+        if (I.eq_kind == 0) bad = !isfinite(cx) || !isfinite(cy);
+        if (bad) atomicOr(&I.dev->err, 1);
         if (isfinite(cx)) spx = rfmax(spx, cx);
         if (isfinite(cy)) spy = rfmax(spy, cy);
       }
@@ -1369,15 +1382,15 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const bool l
         spy = fmax(spy, __shfl_xor_sync(0xffffffffu, spy, o));
       }
       if ((tid & 31) == 0) {
-        atomicMax(&A.dev->smax[A.parity ^ 1][0], (unsigned long long)__double_as_longlong((double)spx));
-        atomicMax(&A.dev->smax[A.parity ^ 1][1], (unsigned long long)__double_as_longlong((double)spy));
+        atomicMax(&I.dev->smax[I.parity ^ 1][0], (unsigned long long)__double_as_longlong((double)spx));
+        atomicMax(&I.dev->smax[I.parity ^ 1][1], (unsigned long long)__double_as_longlong((double)spy));
       }
     } else {
       double mx = block_max((double)spx, red, tid, nthr);
       double my = block_max((double)spy, red, tid, nthr);
       if (tid == 0) {
-        atomicMax(&A.dev->smax[A.parity ^ 1][0], (unsigned long long)__double_as_longlong(mx));
-        atomicMax(&A.dev->smax[A.parity ^ 1][1], (unsigned long long)__double_as_longlong(my));
+        atomicMax(&I.dev->smax[I.parity ^ 1][0], (unsigned long long)__double_as_longlong(mx));
+        atomicMax(&I.dev->smax[I.parity ^ 1][1], (unsigned long long)__double_as_longlong(my));
       }
     }
   }
@@ -1485,8 +1498,8 @@ __global__ void __launch_bounds__(TX *TY / CPT, std::is_same<R, float>::value ? 
     if (t + G < ntiles) stage(col(nxt) * TX, nxt.cy * TY, b ^ 1);
     cp_async_commit();
     R *buf = bufs + b * L.buf;
-    tile_compute<R, K, BASIS, TX, TY, VAR, CPT>(A, lim, col(cur) * TX, cur.cy * TY, buf, flux,
-                                                red, tid, dt, speed, false);
+    tile_compute<R, K, BASIS, TX, TY, VAR, CPT>(A, A, lim, col(cur) * TX, cur.cy * TY, buf,
+                                                flux, red, tid, dt, speed, false);
     cur = nxt;
     advance(nxt);
   }
