@@ -14,27 +14,50 @@ __device__ __forceinline__ void unpack_item(int4 w, int &K, int &TX, int &TY) {
   TY = w.w & 0xfff;
 }
 
-// Stage the item `w` of degree K (instance arguments copied to sA, tile staged into buf)
-// with NT threads.
+// Copy one instance's stage arguments into shared memory: NCH 16-byte cp.async chunks,
+// issued by threads first .. first + step - 1 of the caller's (thread t issues chunks
+// t, t + step, ...).
+template <typename R>
+__device__ __forceinline__ void args_copy_async(const StageArgs<R> *src, StageArgs<R> *dst,
+                                                const int t, const int step) {
+  static_assert(sizeof(StageArgs<R>) % 16 == 0, "16-byte chunks");
+  constexpr int NCH = (int)(sizeof(StageArgs<R>) / 16);
+  for (int c = t; c < NCH; c += step)
+    cp_async<16>(reinterpret_cast<char *>(dst) + 16 * c,
+                 reinterpret_cast<const char *>(src) + 16 * c);
+}
+
+// Stage the tile of item w (its instance's arguments A already in shared memory) into buf,
+// and the instance's time step (k_batch_begin_step computed it once per step) into sdt (by
+// the last thread: the last warp has the fewest face passes).
 template <typename R, int K, int TX, int TY, int NT>
-__device__ __forceinline__ void item_load(const StageArgs<R> *__restrict__ args, const int4 w,
-                                          StageArgs<R> &sA, double &sdt, R *buf, int tid) {
-  constexpr int nthr = NT;
-  static_assert(sizeof(StageArgs<R>) % 4 == 0, "word copy");
-  const int *src = reinterpret_cast<const int *>(args + w.x);
-  for (int k = tid; k < (int)(sizeof(StageArgs<R>) / 4); k += nthr)
-    reinterpret_cast<int *>(&sA)[k] = src[k];
-  const StageArgs<R> &A = args[w.x];
-  // the instance's time step (k_batch_begin_step computed it once per step), staged with
-  // the tile
-  if (tid == 0) cp_async<8>(&sdt, &A.dev->dt[A.parity]);
+__device__ __forceinline__ void item_stage(const StageArgs<R> &A, const int4 &w, double &sdt,
+                                           R *buf, int tid) {
+  if (tid == NT - 1) cp_async<8>(&sdt, &A.dev->dt[A.parity]);
   const bool lim = A.limiter == 1 && A.lim_y && K >= 1;  // the same for the whole group
   tile_load_async<R, K, 1, TX, TY, NT>(A, lim, w.y, w.z, buf, tid);
 }
 
-// Resident CTAs per SM the degree-K batch kernel is compiled for (register budget
-// 65536 / (256 x this)); its shared memory (two staged tiles + the face fluxes) allows it.
-__host__ __device__ constexpr int batch_min_blocks(int K) { return K == 0 ? 4 : K == 1 ? 3 : 2; }
+// Shared-memory bytes of a batch CTA on TX x TY tiles of degree K (with the minmod rows):
+// reduction scratch, two staged tiles, the face fluxes and the three item slots.
+__host__ __device__ constexpr int batch_smem_bytes(int K, int TX, int TY) {
+  return 64 * 8 +
+         4 * (2 * ((NV * num_modes(K, 1) * (TX + 8) * (TY + 2) + NV * 2 * (TX + 8) +
+                    (K + 1) * (TX + 2) + TX + 1 + (K + 1) * (TY + 2) + TY + 1 + 31) &
+                   ~31) +
+              NV * (K + 1) * (TY * (TX + 1) + (TY + 1) * TX)) +
+         3 * ((int)sizeof(StageArgs<float>) + 16 + 8);
+}
+// Resident CTAs per SM the batch kernel is compiled for (its register budget is
+// 65536 / (threads x this)): 4, 3 and 2 for degrees 0, 1 and 2, but never more than the
+// shared memory admits (228 KB per SM, 1 KB of it reserved per CTA), where a higher count
+// would only cap the registers (degree 1 on 32x16 tiles fits two: 122 registers instead
+// of 80 and spills).
+__host__ __device__ constexpr int batch_min_blocks(int K, int TX, int TY) {
+  return (K == 0 ? 4 : K == 1 ? 3 : 2) < 233472 / (batch_smem_bytes(K, TX, TY) + 1024)
+             ? (K == 0 ? 4 : K == 1 ? 3 : 2)
+             : 233472 / (batch_smem_bytes(K, TX, TY) + 1024);
+}
 
 // Persistent batched stage for the items of one group (degree K, TX x TY tiles, CPT cells
 // per thread, one set of physical constants): CTAs stride over the group's work list; the
@@ -47,37 +70,70 @@ __host__ __device__ constexpr int batch_min_blocks(int K) { return K == 0 ? 4 : 
 // item's own arguments (grid, buffers, spacing, equilibrium kind, run state) come from
 // `args`, staged into shared memory with the tile.
 template <typename R, int K, int TX, int TY, bool POS, int CPT>
-__global__ void __launch_bounds__(TX * TY / CPT, batch_min_blocks(K))
+__global__ void __launch_bounds__(TX * TY / CPT, batch_min_blocks(K, TX, TY))
     k_batch_stage(const __grid_constant__ StageArgs<R> Q, const StageArgs<R> *__restrict__ args,
                   const int4 *__restrict__ items, int nitems, int bufsz) {
   constexpr int NT = TX * TY / CPT;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ __align__(16) StageArgs<R> sA[2];  // instance arguments of the staged items
-  __shared__ double sdt[2];                     // and their time steps
+  // Three item slots: the item being computed, the item being staged, and the item whose
+  // descriptor and instance arguments are on their way.  Every per-item value the threads
+  // read comes from shared memory, so no warp waits on a global load at an item's start.
+  __shared__ StageArgs<R> sA[3];      // instance arguments
+  __shared__ __align__(16) int4 sW[3];  // work-list descriptors
+  __shared__ double sdt[3];             // the instances' time steps
   const int tid = threadIdx.x;
   double *red = reinterpret_cast<double *>(smem_raw);
   R *bufs = reinterpret_cast<R *>(smem_raw + 64 * sizeof(double));
   R *flux = bufs + 2 * bufsz;
-  // Item it is staged while item it - G is computed; the barrier after its arrival also
-  // frees the previous item's buffer, argument slot and flux area (as in k_stage).
   const int G = gridDim.x;
   int it = blockIdx.x;
-  if (it < nitems) item_load<R, K, TX, TY, NT>(args, items[it], sA[0], sdt[0], bufs, tid);
+  // prologue: descriptors and arguments of items it and it + G, then item it's tile
+  if (tid < 2 && it + tid * G < nitems) sW[tid] = items[it + tid * G];
+  __syncthreads();
+  for (int j = 0; j < 2; ++j)
+    if (it + j * G < nitems) args_copy_async(args + sW[j].x, &sA[j], tid, NT);
   cp_async_commit();
+  cp_async_wait<0>();
+  __syncthreads();
+  if (it < nitems) item_stage<R, K, TX, TY, NT>(sA[0], sW[0], sdt[0], bufs, tid);
+  cp_async_commit();
+  // Item it (slot s, buffer k & 1) is computed while item it + G (slot s1) is staged; the
+  // descriptor of item it + 2G (slot s2, which item it - G has left) comes by one cp.async
+  // of the last warp's first thread right after the barrier, and the last warp copies that
+  // item's arguments once it has computed its cells.  (The face passes fall unevenly on
+  // the warps -- the first warps take the extra pass of a tile -- so the last warp has time
+  // to spare.)  The barrier after item it's data arrives also frees item it - G's buffer,
+  // slot and the flux area (as in k_stage).
+  constexpr int LW = NT - 32;  // the last warp's first thread
+  int s = 0, s1 = 1, s2 = 2;
   for (int k = 0; it < nitems; it += G, ++k) {
     cp_async_wait<0>();
     __syncthreads();
-    if (it + G < nitems)
-      item_load<R, K, TX, TY, NT>(args, items[it + G], sA[(k + 1) & 1], sdt[(k + 1) & 1],
-                                  bufs + ((k + 1) & 1) * bufsz, tid);
+    const bool more = it + 2 * G < nitems;
+    if (tid == LW && more) cp_async<16>(&sW[s2], &items[it + 2 * G]);
     cp_async_commit();
-    const int4 w = items[it];
-    const StageArgs<R> &I = sA[k & 1];
-    R *buf = bufs + (k & 1) * bufsz;
-    const double dt = sdt[k & 1];
+    if (it + G < nitems)
+      item_stage<R, K, TX, TY, NT>(sA[s1], sW[s1], sdt[s1], bufs + ((k + 1) & 1) * bufsz, tid);
+    cp_async_commit();
     const bool lim = Q.limiter == 1 && Q.lim_y && K >= 1;
     tile_compute<R, K, 1, TX, TY, POS ? WB_VAR_POSITIVITY : 0, CPT>(
-        Q, I, lim, w.y, w.z, buf, flux, red, tid, dt, nullptr, false, true);
+        Q, sA[s], lim, sW[s].y, sW[s].z, bufs + (k & 1) * bufsz, flux, red, tid, sdt[s],
+        nullptr, false, true);
+    if (more && tid >= LW) {
+      // thread LW's descriptor copy is its second-newest group (the staging is the newest)
+      int x = 0;
+      if (tid == LW) {
+        cp_async_wait<1>();
+        x = sW[s2].x;
+      }
+      x = __shfl_sync(0xffffffffu, x, 0);
+      args_copy_async(args + x, &sA[s2], tid - LW, 32);
+      cp_async_commit();
+    }
+    const int t0 = s;
+    s = s1;
+    s1 = s2;
+    s2 = t0;
   }
   cp_async_wait<0>();
 }

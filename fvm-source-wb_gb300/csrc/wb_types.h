@@ -78,8 +78,10 @@ struct Combo {
 constexpr int WB_VAR_POSITIVITY = 1;  // Zhang-Shu positivity limiter (limiter 2)
 constexpr int WB_VAR_HLLC = 2;        // HLLC face flux instead of LLF
 
+// 16-byte aligned (and sized): the batched form copies it into shared memory in 16-byte
+// chunks.
 template <typename R>
-struct StageArgs {
+struct alignas(16) StageArgs {
   const R *x;                 // stage input (loaded with halo, limited if lim_y)
   Combo<R> o[2];              // o[1].out may be null
   int nx, ny;
