@@ -53,6 +53,7 @@ struct wb_batch {
   StageArgs<float> *args = nullptr;  // [6 phases][2 stages][n]
   std::vector<StageArgs<float>> hargs;  // host copy of args (the groups' launch constants)
   const float **state_ptrs = nullptr;  // [6 phases][n] current state per phase
+  int *errs = nullptr;                 // [n] the instances' device error words (wb_batch_sync)
   int phase = 0;
   int dt_mode = -1;
   double dt = 0.0;
@@ -265,6 +266,7 @@ int wb_batch_destroy(wb_batch *b) {
   cudaFree(b->items);
   cudaFree(b->args);
   cudaFree(b->state_ptrs);
+  cudaFree(b->errs);
   for (wb_ctx *c : b->inst) wb_destroy(c);
   for (int k = 0; k < wb_batch::kMaxBranches; ++k) {
     if (b->branch[k]) cudaStreamDestroy(b->branch[k]);
@@ -338,6 +340,7 @@ int wb_batch_create(const wb_config *cfgs, int32_t n, wb_batch **out) {
   if (rc) return rc;
   BCK(cudaMalloc(&b->args, (size_t)6 * 2 * n * sizeof(StageArgs<float>)));
   BCK(cudaMalloc(&b->state_ptrs, (size_t)6 * n * sizeof(float *)));
+  BCK(cudaMalloc(&b->errs, (size_t)n * sizeof(int)));
   return build_args(b, 1, 0.0);
 }
 
@@ -474,10 +477,21 @@ int wb_batch_autotune(wb_batch *b, int32_t reps, int32_t *tiles) {
 int wb_batch_sync(wb_batch *b) {
   if (!b) return WB_ERR_ARG;
   BCK(cudaSetDevice(b->device));
+  // every instance's error word in one launch and one copy (a synchronous read per instance
+  // costs about 10 us each: milliseconds for a batch of hundreds)
+  const int n = (int)b->inst.size();
+  std::vector<int> e(n);
+  BCK(launch_batch_errors(b->args, n, b->errs, b->stream));
+  BCK(cudaMemcpyAsync(e.data(), b->errs, n * sizeof(int), cudaMemcpyDeviceToHost, b->stream));
   BCK(cudaStreamSynchronize(b->stream));
-  for (size_t i = 0; i < b->inst.size(); ++i) {
-    int rc = wb_sync(b->inst[i]);
-    if (rc) return berr(b, rc, std::string("instance ") + std::to_string(i) + ": " + wb_last_error(b->inst[i]));
+  for (int i = 0; i < n; ++i) {
+    if (e[i] & 2)
+      return berr(b, WB_ERR_TIMEOUT, "instance " + std::to_string(i) +
+                                         ": a bounded device wait (tile copy) gave up");
+    if (e[i])
+      return berr(b, WB_ERR_NONPHYSICAL,
+                  "instance " + std::to_string(i) +
+                      ": non-finite or non-positive density/pressure in a cell mean");
   }
   return WB_OK;
 }

@@ -158,6 +158,15 @@ __global__ void __launch_bounds__(128) k_batch_begin_step(const StageArgs<R> *__
   S->smax[A.parity ^ 1][1] = 0ull;
 }
 
+// Every instance's device error word into out[i] (one small copy back for the whole batch
+// instead of one synchronous copy per instance).
+template <typename R>
+__global__ void __launch_bounds__(128) k_batch_errors(const StageArgs<R> *__restrict__ args, int n,
+                                                      int *out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = args[i].dev->err;
+}
+
 // Per-instance wave-speed maxima of the cell means into dev->smax[parity] (the batched
 // compute_max_speed), over the same work list.
 template <typename R>

@@ -67,6 +67,8 @@ bool batch_tile_supported(int order, int tx, int ty, int cpt);
 int batch_tile_candidates(int order, int (*out)[3], int max);
 cudaError_t launch_batch_max_speed(const StageArgs<float> *args, const float *const *state,
                                    const int4 *items, int nitems, cudaStream_t s);
+// every instance's device error word into out[0 .. n)
+cudaError_t launch_batch_errors(const StageArgs<float> *args, int n, int *out, cudaStream_t s);
 // start of a step for the n instances (time step, time, step count, next speed slots)
 cudaError_t launch_batch_begin_step(const StageArgs<float> *args, int n, cudaStream_t s);
 

@@ -16,6 +16,11 @@ cudaError_t launch_batch_begin_step(const StageArgs<float> *args, int n, cudaStr
   return cudaGetLastError();
 }
 
+cudaError_t launch_batch_errors(const StageArgs<float> *args, int n, int *out, cudaStream_t s) {
+  k_batch_errors<float><<<(n + 127) / 128, 128, 0, s>>>(args, n, out);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_batch_max_speed(const StageArgs<float> *args, const float *const *state,
                                    const int4 *items, int nitems, cudaStream_t s) {
   int grid = nitems < 4096 ? nitems : 4096;

@@ -263,6 +263,9 @@ const char *wb_batch_last_error(const wb_batch *b);
 int wb_batch_init_perturbation(wb_batch *b, const wb_perturbation *ics);
 /* nsteps steps; each instance takes its own CFL dt (dt <= 0) or the fixed dt */
 int wb_batch_step(wb_batch *b, int32_t nsteps, double dt);
+/* Waits for the batch's work and checks every instance's device error word (one copy for
+ * the whole batch): WB_ERR_NONPHYSICAL or WB_ERR_TIMEOUT, with the first failing instance
+ * named in wb_batch_last_error. */
 int wb_batch_sync(wb_batch *b);
 /* Tile autotuner of the batched form: for every (degree, size class) group of instances
  * without a pinned tile -- size class 0: max(nx, ny) < 128, 1: the rest -- times `reps`

@@ -57,6 +57,20 @@ def test_batch_mixed_physics_matches_single_instances(wb):
         np.testing.assert_array_equal(outs[i], ref, err_msg="instance %d" % i)
 
 
+def test_batch_sync_names_the_nonphysical_instance(wb):
+    """wb_batch_sync reads every instance's device error word in one copy and reports the
+    first instance whose cell means went non-physical."""
+    cfgs, ics = wb.batch_workload(n=4, seed_base=31, nmin=24, nmax=40)
+    ics[2].amp = -5.0  # the pressure bump drives the centre's pressure below zero
+    with wb.Batch(cfgs) as b:
+        b.init_perturbation(ics)
+        b.step(2, 1e-4)
+        with pytest.raises(wb.WbError) as ei:
+            b.sync()
+    assert ei.value.status == wb.WB_ERR_NONPHYSICAL
+    assert "instance 2" in str(ei.value)
+
+
 def test_batch_zero_perturbation_stays_zero(wb):
     cfgs, ics = wb.batch_workload(n=6, seed_base=5, nmin=16, nmax=40)
     for ic in ics:
