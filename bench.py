@@ -223,13 +223,14 @@ def parse_batch_tiles(spec):
     return out
 
 
-def batch_leg(wb, n, dev, steps=24, warmup=6, pinned=None):
+def batch_leg(wb, n, dev, steps=24, warmup=6, pinned=None, instances=None, label=None):
     """The batched form on n instances: DOF-updates/s over `steps` CFL steps (host clock
     around graph launches + sync, after `warmup` steps that include the graph capture), and
     its HBM roofline fraction (20 B per DOF-update per SSP-RK2 step, all stage launches).
     pinned: {degree: (TX, TY, CPT)} pins those degrees' tiles (profiling); the rest are
-    autotuned."""
-    cfgs, ics = wb.batch_workload(n=n, device=dev)
+    autotuned.  instances: (configs, initial conditions) instead of the cfg4 draw, named by
+    label."""
+    cfgs, ics = instances if instances else wb.batch_workload(n=n, device=dev)
     for c in cfgs:
         if pinned and c.order in pinned:
             c.tile_x, c.tile_y, c.cells_per_thread = pinned[c.order]
@@ -254,9 +255,10 @@ def batch_leg(wb, n, dev, steps=24, warmup=6, pinned=None):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
                          "kernel": "k_batch_stage<float>", "note": "whole step, host clock"},
-            "workload": "%d instances: N = exp(U(ln 32, ln 512)), degree 0..2 (P basis), "
-                        "isothermal or polytrope, Gaussian bump 10^U(-6,-2); FP32, SSP-RK2, "
-                        "CFL steps" % len(cfgs)}
+            "workload": label or (
+                "%d instances: N = exp(U(ln 32, ln 512)), degree 0..2 (P basis), "
+                "isothermal or polytrope, Gaussian bump 10^U(-6,-2); FP32, SSP-RK2, "
+                "CFL steps" % len(cfgs))}
 
 
 def batch_accuracy(wb, n, dev, steps=20):
@@ -327,8 +329,18 @@ def limited_leg(wb, name, dev, steps=6, warmup=3):
 def run_batch_only(args):
     wb = load_package()
     line = {"metric": "batched form: " + UNIT, "impl": "batch"}
+    instances, label = None, None
+    if args.batch_grid:
+        # one instance: the workload's grid (at --nx), to set the batch kernel beside
+        # k_stage on the same cells
+        n = args.nx or wb.workload(args.workload)["nx"]
+        c = wb.default_config(**wb.workload(args.workload, nx=n, ny=n))
+        instances = ([c], [wb.workload_ic(args.workload)])
+        label = "one instance: the %s grid at %dx%d (FP32, SSP-RK2, CFL steps)" % (
+            args.workload, n, n)
     line.update(batch_leg(wb, args.batch, 0, steps=args.steps, warmup=max(args.warmup, 6),
-                          pinned=parse_batch_tiles(args.batch_tiles)))
+                          pinned=parse_batch_tiles(args.batch_tiles), instances=instances,
+                          label=label))
     print(json.dumps(line))
     return 0
 
@@ -577,6 +589,8 @@ def main():
     ap.add_argument("--accuracy-steps", type=int, default=500)
     ap.add_argument("--batch", type=int, default=0,
                     help="run only the batched form with this many instances (profiling)")
+    ap.add_argument("--batch-grid", action="store_true",
+                    help="with --batch 1: the one instance is the workload's grid (at --nx)")
     ap.add_argument("--batch-tiles", default="",
                     help="with --batch: pin tiles per degree, e.g. 0:32x16/2,1:32x16/2,2:32x8/1")
     args = ap.parse_args()
