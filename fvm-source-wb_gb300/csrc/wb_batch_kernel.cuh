@@ -7,9 +7,11 @@
 
 namespace wb {
 
-// item = {instance, i0, j0, (K << 24) | (TX << 12) | TY}
+// item = {instance, i0, j0, (interior << 30) | (K << 24) | (TX << 12) | TY}; interior: the
+// tile's staged block lies inside the grid (tma_tile), so a TMA copy can stage its modes
+__device__ __forceinline__ bool item_interior(int4 w) { return (w.w >> 30) & 1; }
 __device__ __forceinline__ void unpack_item(int4 w, int &K, int &TX, int &TY) {
-  K = (w.w >> 24) & 0xff;
+  K = (w.w >> 24) & 0x3f;
   TX = (w.w >> 12) & 0xfff;
   TY = w.w & 0xfff;
 }
@@ -27,15 +29,39 @@ __device__ __forceinline__ void args_copy_async(const StageArgs<R> *src, StageAr
                  reinterpret_cast<const char *>(src) + 16 * c);
 }
 
+// A tensor map in global memory, written there by a host copy, made visible to the
+// tensor-map proxy of the calling thread before its TMA copies use it, and fetched into
+// the descriptor cache ahead of them.
+__device__ __forceinline__ void tensormap_acquire(const CUtensorMap *m) {
+  asm volatile("fence.proxy.tensormap::generic.acquire.sys [%0], 128;\n" ::"l"(m) : "memory");
+  asm volatile("prefetch.tensormap [%0];\n" ::"l"(m) : "memory");
+}
+
 // Stage the tile of item w (its instance's arguments A already in shared memory) into buf,
-// and the instance's time step (k_batch_begin_step computed it once per step) into sdt (by
-// the last thread: the last warp has the fewest face passes).
+// and the instance's time step (k_batch_begin_step computed it once per step) into sdt.
+// An interior tile's modes come by one TMA copy through the instance's tensor map (when
+// use_tma; thread NT - 32 acquired that map when the item's descriptor arrived).  `bar` (the buffer's mbarrier, one arrival per phase) gets exactly one arrival
+// per item -- with the TMA byte count, or a plain one when the tile comes by cp.async -- so
+// its phase parity for the j-th item in the buffer is j & 1 and no thread keeps any other
+// record.  The bookkeeping is the last warp's: it has the fewest face passes.
 template <typename R, int K, int TX, int TY, int NT>
 __device__ __forceinline__ void item_stage(const StageArgs<R> &A, const int4 &w, double &sdt,
-                                           R *buf, int tid) {
+                                           R *buf, unsigned long long *bar,
+                                           const CUtensorMap *__restrict__ tmaps,
+                                           const int use_tma, int tid) {
   if (tid == NT - 1) cp_async<8>(&sdt, &A.dev->dt[A.parity]);
   const bool lim = A.limiter == 1 && A.lim_y && K >= 1;  // the same for the whole group
-  tile_load_async<R, K, 1, TX, TY, NT>(A, lim, w.y, w.z, buf, tid);
+  const bool tma = item_interior(w) && tma_tile<TX, TY>(use_tma, A.nx, A.ny, w.y, w.z);
+  if (tid == NT - 32) {
+    if (tma) {
+      constexpr unsigned bytes = NV * num_modes(K, 1) * (TY + 2) * (TX + 8) * sizeof(R);
+      mbar_expect_tx(bar, bytes);
+      tma_load_3d(buf, tmaps + w.x, w.y - 4, w.z - 1, 0, bar);  // the modes start the buffer
+    } else {
+      mbar_arrive(bar);
+    }
+  }
+  tile_load_async<R, K, 1, TX, TY, NT>(A, lim, w.y, w.z, buf, tid, !tma);
 }
 
 // Shared-memory bytes of a batch CTA on TX x TY tiles of degree K (with the minmod rows):
@@ -46,7 +72,7 @@ __host__ __device__ constexpr int batch_smem_bytes(int K, int TX, int TY) {
                     (K + 1) * (TX + 2) + TX + 1 + (K + 1) * (TY + 2) + TY + 1 + 31) &
                    ~31) +
               NV * (K + 1) * (TY * (TX + 1) + (TY + 1) * TX)) +
-         3 * ((int)sizeof(StageArgs<float>) + 16 + 8);
+         3 * ((int)sizeof(StageArgs<float>) + 16 + 8) + 16;
 }
 // Resident CTAs per SM the batch kernel is compiled for (its register budget is
 // 65536 / (threads x this)): 4, 3 and 2 for degrees 0, 1 and 2, but never more than the
@@ -72,30 +98,48 @@ __host__ __device__ constexpr int batch_min_blocks(int K, int TX, int TY) {
 template <typename R, int K, int TX, int TY, bool POS, int CPT>
 __global__ void __launch_bounds__(TX * TY / CPT, batch_min_blocks(K, TX, TY))
     k_batch_stage(const __grid_constant__ StageArgs<R> Q, const StageArgs<R> *__restrict__ args,
-                  const int4 *__restrict__ items, int nitems, int bufsz) {
+                  const CUtensorMap *__restrict__ tmaps, const int4 *__restrict__ items,
+                  int nitems, int bufsz) {
   constexpr int NT = TX * TY / CPT;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   // Three item slots: the item being computed, the item being staged, and the item whose
   // descriptor and instance arguments are on their way.  Every per-item value the threads
   // read comes from shared memory, so no warp waits on a global load at an item's start.
   __shared__ StageArgs<R> sA[3];      // instance arguments
   __shared__ __align__(16) int4 sW[3];  // work-list descriptors
   __shared__ double sdt[3];             // the instances' time steps
+  __shared__ unsigned long long bar[2];  // one arrival per item staged into buffer b
   const int tid = threadIdx.x;
   double *red = reinterpret_cast<double *>(smem_raw);
   R *bufs = reinterpret_cast<R *>(smem_raw + 64 * sizeof(double));
   R *flux = bufs + 2 * bufsz;
+  // TMA destinations must be 128-byte aligned: checked, never assumed (kernel constants
+  // only, so the flag need not stay in a register)
+#define WB_BATCH_USE_TMA                                                                 \
+  (Q.use_tma && tmaps != nullptr && (smem_u32(bufs) & 127u) == 0u &&                     \
+   ((bufsz * (int)sizeof(R)) & 127) == 0)
   const int G = gridDim.x;
-  int it = blockIdx.x;
+  const int it = blockIdx.x;
   // prologue: descriptors and arguments of items it and it + G, then item it's tile
   if (tid < 2 && it + tid * G < nitems) sW[tid] = items[it + tid * G];
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_fence_init();
+  }
   __syncthreads();
   for (int j = 0; j < 2; ++j)
-    if (it + j * G < nitems) args_copy_async(args + sW[j].x, &sA[j], tid, NT);
+    if (it + j * G < nitems) {
+      args_copy_async(args + sW[j].x, &sA[j], tid, NT);
+      if (tid == NT - 32 && WB_BATCH_USE_TMA && item_interior(sW[j]))
+        tensormap_acquire(tmaps + sW[j].x);
+    }
   cp_async_commit();
   cp_async_wait<0>();
   __syncthreads();
-  if (it < nitems) item_stage<R, K, TX, TY, NT>(sA[0], sW[0], sdt[0], bufs, tid);
+  if (it < nitems)
+    item_stage<R, K, TX, TY, NT>(sA[0], sW[0], sdt[0], bufs, &bar[0], tmaps, WB_BATCH_USE_TMA,
+                                 tid);
   cp_async_commit();
   // Item it (slot s, buffer k & 1) is computed while item it + G (slot s1) is staged; the
   // descriptor of item it + 2G (slot s2, which item it - G has left) comes by one cp.async
@@ -105,37 +149,44 @@ __global__ void __launch_bounds__(TX * TY / CPT, batch_min_blocks(K, TX, TY))
   // to spare.)  The barrier after item it's data arrives also frees item it - G's buffer,
   // slot and the flux area (as in k_stage).
   constexpr int LW = NT - 32;  // the last warp's first thread
-  int s = 0, s1 = 1, s2 = 2;
-  for (int k = 0; it < nitems; it += G, ++k) {
+  // Only k is carried across the compute body (registers are what the body lacks): the
+  // item, its slot and its buffer follow from it.
+  for (int k = 0; blockIdx.x + k * G < nitems; ++k) {
+    const int it = blockIdx.x + k * G, s = k % 3, s1 = (k + 1) % 3;
     cp_async_wait<0>();
-    __syncthreads();
-    const bool more = it + 2 * G < nitems;
-    if (tid == LW && more) cp_async<16>(&sW[s2], &items[it + 2 * G]);
+    // item it is the (k >> 1)-th of buffer k & 1; a wait that gives up stops the CTA
+    const bool bad = !mbar_wait(&bar[k & 1], (k >> 1) & 1);
+    if (bad && tid == 0) atomicOr(&sA[s].dev->err, 2);
+    if (__syncthreads_or(bad)) {
+      (void)mbar_wait(&bar[k & 1], (k >> 1) & 1);  // nothing may still be copying at exit
+      break;
+    }
+    if (tid == LW && it + 2 * G < nitems) cp_async<16>(&sW[(k + 2) % 3], &items[it + 2 * G]);
     cp_async_commit();
     if (it + G < nitems)
-      item_stage<R, K, TX, TY, NT>(sA[s1], sW[s1], sdt[s1], bufs + ((k + 1) & 1) * bufsz, tid);
+      item_stage<R, K, TX, TY, NT>(sA[s1], sW[s1], sdt[s1], bufs + ((k + 1) & 1) * bufsz,
+                                   &bar[(k + 1) & 1], tmaps, WB_BATCH_USE_TMA, tid);
     cp_async_commit();
     const bool lim = Q.limiter == 1 && Q.lim_y && K >= 1;
     tile_compute<R, K, 1, TX, TY, POS ? WB_VAR_POSITIVITY : 0, CPT>(
         Q, sA[s], lim, sW[s].y, sW[s].z, bufs + (k & 1) * bufsz, flux, red, tid, sdt[s],
         nullptr, false, true);
-    if (more && tid >= LW) {
+    if (tid >= LW && blockIdx.x + (k + 2) * G < nitems) {
       // thread LW's descriptor copy is its second-newest group (the staging is the newest)
+      const int s2 = (k + 2) % 3;
       int x = 0;
       if (tid == LW) {
         cp_async_wait<1>();
         x = sW[s2].x;
+        if (WB_BATCH_USE_TMA && item_interior(sW[s2])) tensormap_acquire(tmaps + x);
       }
       x = __shfl_sync(0xffffffffu, x, 0);
       args_copy_async(args + x, &sA[s2], tid - LW, 32);
       cp_async_commit();
     }
-    const int t0 = s;
-    s = s1;
-    s1 = s2;
-    s2 = t0;
   }
   cp_async_wait<0>();
+#undef WB_BATCH_USE_TMA
 }
 
 // Start of a step, one thread per instance: the step's time step (stage_dt, whose FP64

@@ -12,8 +12,8 @@ namespace wb {
 
 template <int K, int TX, int TY, bool POS, int CPT>
 static cudaError_t launch_batch_stage_t(const StageArgs<float> &Q, const StageArgs<float> *args,
-                                        const int4 *items, int nitems, int bufsz, size_t smem,
-                                        int *grid_out, cudaStream_t s) {
+                                        const CUtensorMap *tmaps, const int4 *items, int nitems,
+                                        int bufsz, size_t smem, int *grid_out, cudaStream_t s) {
   constexpr int NT = TX * TY / CPT;  // threads per CTA
   auto kern = k_batch_stage<float, K, TX, TY, POS, CPT>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -26,7 +26,7 @@ static cudaError_t launch_batch_stage_t(const StageArgs<float> &Q, const StageAr
   int grid = nsm * (per_sm > 0 ? per_sm : 1);
   if (grid > nitems) grid = nitems;
   if (grid_out) *grid_out = grid;
-  kern<<<grid, NT, smem, s>>>(Q, args, items, nitems, bufsz);
+  kern<<<grid, NT, smem, s>>>(Q, args, tmaps, items, nitems, bufsz);
   return cudaGetLastError();
 }
 
@@ -35,9 +35,9 @@ static cudaError_t launch_batch_stage_t(const StageArgs<float> &Q, const StageAr
 #define WB_BATCH_INSTANCE(K, TX, TY, POS, CPT)                                               \
   namespace wb {                                                                            \
   cudaError_t WB_BATCH_INSTANCE_NAME(K, TX, TY, POS, CPT)(                                  \
-      const StageArgs<float> &Q, const StageArgs<float> *args, const int4 *items,           \
-      int nitems, int bufsz, size_t smem, int *grid_out, cudaStream_t s) {                  \
-    return launch_batch_stage_t<K, TX, TY, POS != 0, CPT>(Q, args, items, nitems, bufsz,    \
-                                                         smem, grid_out, s);                \
+      const StageArgs<float> &Q, const StageArgs<float> *args, const CUtensorMap *tmaps,    \
+      const int4 *items, int nitems, int bufsz, size_t smem, int *grid_out, cudaStream_t s) { \
+    return launch_batch_stage_t<K, TX, TY, POS != 0, CPT>(Q, args, tmaps, items, nitems,    \
+                                                         bufsz, smem, grid_out, s);         \
   }                                                                                         \
   }

@@ -1372,6 +1372,9 @@ int ctx_rk2_stage_args(wb_ctx *ctx, int phase, int dt_mode, double dt, StageArgs
   return WB_OK;
 }
 const float *ctx_state_f32(wb_ctx *c) { return (const float *)state_buf(c, 0); }
+const CUtensorMap *ctx_state_tmap(wb_ctx *c, const void *base, int TX, int TY) {
+  return state_tmap(c, base, TX, TY);
+}
 DevState *ctx_dev_state(wb_ctx *c) { return c->dev; }
 void ctx_tile(wb_ctx *c, int *tx, int *ty, int *cpt) {
   *tx = c->TX;

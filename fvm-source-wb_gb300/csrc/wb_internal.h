@@ -59,9 +59,12 @@ cudaError_t launch_copy_device(void *out, const void *in, size_t bytes, cudaStre
 
 // batched form (FP32): persistent stage over a work list (Q: the group's shared constants,
 // args: every instance's arguments); per-instance max speed
+// tmaps: the instances' tensor maps of the staged input on the group's tile (indexed like
+// args), used when Q.use_tma
 cudaError_t launch_batch_stage(const StageArgs<float> &Q, const StageArgs<float> *args,
-                               const int4 *items, int nitems, int bufsz, size_t smem, int pos,
-                               int K, int TX, int TY, int CPT, int *grid_out, cudaStream_t s);
+                               const CUtensorMap *tmaps, const int4 *items, int nitems,
+                               int bufsz, size_t smem, int pos, int K, int TX, int TY, int CPT,
+                               int *grid_out, cudaStream_t s);
 // the tile shapes (TX, TY, cells per thread) the batch kernels compile for degree K
 bool batch_tile_supported(int order, int tx, int ty, int cpt);
 int batch_tile_candidates(int order, int (*out)[3], int max);
@@ -82,6 +85,9 @@ int ctx_create(const wb_config *cfg, int row_align, wb_ctx **out);
 // RK2 stage arguments of a context for step phase p (0..5: buffer rotation mod 3 and
 // parity mod 2, counted from the context's current position); FP32 contexts only.
 int ctx_rk2_stage_args(wb_ctx *c, int phase, int dt_mode, double dt, StageArgs<float> out[2]);
+// the tensor map staging TX x TY tiles (with halo) of the context's state buffer `base`;
+// null where TMA cannot address it or is disabled (WB_NO_TMA=1)
+const CUtensorMap *ctx_state_tmap(wb_ctx *c, const void *base, int TX, int TY);
 // device address of the current state and of the context's run state
 const float *ctx_state_f32(wb_ctx *c);
 DevState *ctx_dev_state(wb_ctx *c);

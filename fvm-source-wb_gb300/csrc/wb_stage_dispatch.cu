@@ -18,8 +18,8 @@ WB_STAGE_INSTANCES(WB_DECL)
 #undef WB_DECL
 #define WB_BDECL(K, TX, TY, POS, CPT)                                                         \
   cudaError_t WB_BATCH_INSTANCE_NAME(K, TX, TY, POS, CPT)(                                  \
-      const StageArgs<float> &Q, const StageArgs<float> *args, const int4 *items,           \
-      int nitems, int bufsz, size_t smem, int *grid_out, cudaStream_t s);
+      const StageArgs<float> &Q, const StageArgs<float> *args, const CUtensorMap *tmaps,    \
+      const int4 *items, int nitems, int bufsz, size_t smem, int *grid_out, cudaStream_t s);
 WB_BATCH_INSTANCES(WB_BDECL)
 #undef WB_BDECL
 
@@ -111,13 +111,14 @@ int tile_candidates(int precision_fp32, int order, int basis, int (*out)[3], int
 }
 
 cudaError_t launch_batch_stage(const StageArgs<float> &Q, const StageArgs<float> *args,
-                               const int4 *items, int nitems, int bufsz, size_t smem, int pos,
-                               int K, int TX, int TY, int CPT, int *grid_out, cudaStream_t s) {
+                               const CUtensorMap *tmaps, const int4 *items, int nitems,
+                               int bufsz, size_t smem, int pos, int K, int TX, int TY, int CPT,
+                               int *grid_out, cudaStream_t s) {
   const int p = pos && K >= 1 ? 1 : 0;
 #define WB_BCASE(K_, TX_, TY_, POS_, CPT_)                                                    \
   if (K == K_ && TX == TX_ && TY == TY_ && p == POS_ && CPT == CPT_)                         \
-    return WB_BATCH_INSTANCE_NAME(K_, TX_, TY_, POS_, CPT_)(Q, args, items, nitems, bufsz,   \
-                                                           smem, grid_out, s);
+    return WB_BATCH_INSTANCE_NAME(K_, TX_, TY_, POS_, CPT_)(Q, args, tmaps, items, nitems,   \
+                                                           bufsz, smem, grid_out, s);
   WB_BATCH_INSTANCES(WB_BCASE)
 #undef WB_BCASE
   return cudaErrorInvalidValue;
