@@ -120,6 +120,14 @@ extern "C" int wb_norms_device_noalloc(int32_t nx, int32_t ny, int32_t order, in
   const long long nbx = (nx + 31) / 32, nby = (ny + 7) / 8;
   if ((long long)nx * ny > WB_NORMS_NOALLOC_MAX_CELLS || nbx * nby > kMaxBlocks)
     return WB_ERR_ARG;  // larger than the fixed scratch: use wb_norms
+  // every call copies its results back and waits for the stream, which a stream capture
+  // does not allow: refuse before touching the caller's capture
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(static_cast<cudaStream_t>(stream), &cs) != cudaSuccess) {
+    cudaGetLastError();
+    return WB_ERR_CUDA;
+  }
+  if (cs != cudaStreamCaptureStatusNone) return WB_ERR_ARG;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
     cudaGetLastError();

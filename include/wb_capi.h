@@ -222,8 +222,10 @@ int wb_conserved_sums(wb_ctx *ctx, double sums[4]);
  * WB_NORMS_NOALLOC_MAX_CELLS cells, and a grid whose 32x8-cell blocks outnumber the
  * array's 16,384 partial slots (a narrow grid such as 33 x 127,000) returns WB_ERR_ARG too
  * (use wb_norms).  The first call on a device sets that device up (looks up the array's
- * device address and uploads the basis tables): make the first call before any stream
- * capture.  The set-up belongs to the device's CUDA context: after that context is torn
+ * device address and uploads the basis tables).  Every call copies its results back and
+ * waits for `stream`, so no call may be made while that stream is being captured into a
+ * graph: such a call returns WB_ERR_ARG and leaves the capture as it was.  The set-up
+ * belongs to the device's CUDA context: after that context is torn
  * down (cudaDeviceReset) and created again, the next call sets the device up again.  Every call
  * uses the same array, so calls that overlap on the GPU (other streams, other threads)
  * race.  stream may be NULL (the default stream); the call waits for it before it returns

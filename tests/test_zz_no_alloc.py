@@ -101,3 +101,30 @@ def test_noalloc_rejects_narrow_grids_with_too_many_blocks(wb):
         rc = f(33, 127000, 1, 1, 1.0, 1.0, pa, None, 33 * 127000, None, _ptr(l1), _ptr(linf),
                _ptr(l2))
         assert rc == wb.WB_ERR_ARG
+
+
+def test_noalloc_refuses_a_capturing_stream(wb):
+    """A call on a stream that is being captured into a graph returns WB_ERR_ARG (the call
+    copies its results back and waits, which a capture does not allow) and leaves the
+    capture intact: the graph still instantiates and replays."""
+    torch = pytest.importorskip("torch")
+    f = _entry(wb)
+    c = base_cfg(nx=8, ny=8, order=1, basis=1)
+    with solver(wb, c, 0) as a:
+        pa, plane = a.device_state()
+        l1, linf, l2 = np.zeros(4), np.zeros(4), np.zeros(4)
+        x = torch.zeros(16, device="cuda:0")
+        s = torch.cuda.Stream(device="cuda:0")
+        s.wait_stream(torch.cuda.current_stream())
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(s):
+            g.capture_begin()
+            x.add_(1.0)
+            rc = f(8, 8, 1, 1, 1.0, 1.0, pa, None, plane, ctypes.c_void_p(s.cuda_stream),
+                   _ptr(l1), _ptr(linf), _ptr(l2))
+            x.add_(1.0)
+            g.capture_end()
+        assert rc == wb.WB_ERR_ARG
+        g.replay()
+        torch.cuda.synchronize()
+        assert float(x.sum().item()) == 32.0
