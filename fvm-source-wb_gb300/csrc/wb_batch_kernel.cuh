@@ -40,10 +40,11 @@ __device__ __forceinline__ void tensormap_acquire(const CUtensorMap *m) {
 // Stage the tile of item w (its instance's arguments A already in shared memory) into buf,
 // and the instance's time step (k_batch_begin_step computed it once per step) into sdt.
 // An interior tile's modes come by one TMA copy through the instance's tensor map (when
-// use_tma; thread NT - 32 acquired that map when the item's descriptor arrived).  `bar` (the buffer's mbarrier, one arrival per phase) gets exactly one arrival
-// per item -- with the TMA byte count, or a plain one when the tile comes by cp.async -- so
-// its phase parity for the j-th item in the buffer is j & 1 and no thread keeps any other
-// record.  The bookkeeping is the last warp's: it has the fewest face passes.
+// use_tma; thread NT - 32 acquired that map when the item's descriptor arrived).  `bar`
+// (the buffer's mbarrier, one arrival per phase) gets exactly one arrival per item -- with
+// the TMA byte count, or a plain one when the tile comes by cp.async -- so its phase parity
+// for the j-th item in the buffer is j & 1 and no thread keeps any other record.  The
+// bookkeeping is the last warp's: it has the fewest face passes.
 template <typename R, int K, int TX, int TY, int NT>
 __device__ __forceinline__ void item_stage(const StageArgs<R> &A, const int4 &w, double &sdt,
                                            R *buf, unsigned long long *bar,
@@ -85,6 +86,16 @@ __host__ __device__ constexpr int batch_min_blocks(int K, int TX, int TY) {
              : 233472 / (batch_smem_bytes(K, TX, TY) + 1024);
 }
 
+// Whether a batch launch stages interior items by TMA: tensor maps given, and the staging
+// buffers 128-byte aligned as TMA destinations must be (checked, never assumed).  Kernel
+// constants only, so it is recomputed where used rather than held in a register.
+template <typename R>
+__device__ __forceinline__ bool batch_tma_ok(const StageArgs<R> &Q, const CUtensorMap *tmaps,
+                                             const R *bufs, int bufsz) {
+  return Q.use_tma && tmaps != nullptr && (smem_u32(bufs) & 127u) == 0u &&
+         ((bufsz * (int)sizeof(R)) & 127) == 0;
+}
+
 // Persistent batched stage for the items of one group (degree K, TX x TY tiles, CPT cells
 // per thread, one set of physical constants): CTAs stride over the group's work list; the
 // next item is staged (cp.async) while the current one is computed.  bufsz = the largest
@@ -113,11 +124,6 @@ __global__ void __launch_bounds__(TX * TY / CPT, batch_min_blocks(K, TX, TY))
   double *red = reinterpret_cast<double *>(smem_raw);
   R *bufs = reinterpret_cast<R *>(smem_raw + 64 * sizeof(double));
   R *flux = bufs + 2 * bufsz;
-  // TMA destinations must be 128-byte aligned: checked, never assumed (kernel constants
-  // only, so the flag need not stay in a register)
-#define WB_BATCH_USE_TMA                                                                 \
-  (Q.use_tma && tmaps != nullptr && (smem_u32(bufs) & 127u) == 0u &&                     \
-   ((bufsz * (int)sizeof(R)) & 127) == 0)
   const int G = gridDim.x;
   const int it = blockIdx.x;
   // prologue: descriptors and arguments of items it and it + G, then item it's tile
@@ -131,15 +137,15 @@ __global__ void __launch_bounds__(TX * TY / CPT, batch_min_blocks(K, TX, TY))
   for (int j = 0; j < 2; ++j)
     if (it + j * G < nitems) {
       args_copy_async(args + sW[j].x, &sA[j], tid, NT);
-      if (tid == NT - 32 && WB_BATCH_USE_TMA && item_interior(sW[j]))
+      if (tid == NT - 32 && batch_tma_ok(Q, tmaps, bufs, bufsz) && item_interior(sW[j]))
         tensormap_acquire(tmaps + sW[j].x);
     }
   cp_async_commit();
   cp_async_wait<0>();
   __syncthreads();
   if (it < nitems)
-    item_stage<R, K, TX, TY, NT>(sA[0], sW[0], sdt[0], bufs, &bar[0], tmaps, WB_BATCH_USE_TMA,
-                                 tid);
+    item_stage<R, K, TX, TY, NT>(sA[0], sW[0], sdt[0], bufs, &bar[0], tmaps,
+                                 batch_tma_ok(Q, tmaps, bufs, bufsz), tid);
   cp_async_commit();
   // Item it (slot s, buffer k & 1) is computed while item it + G (slot s1) is staged; the
   // descriptor of item it + 2G (slot s2, which item it - G has left) comes by one cp.async
@@ -165,7 +171,8 @@ __global__ void __launch_bounds__(TX * TY / CPT, batch_min_blocks(K, TX, TY))
     cp_async_commit();
     if (it + G < nitems)
       item_stage<R, K, TX, TY, NT>(sA[s1], sW[s1], sdt[s1], bufs + ((k + 1) & 1) * bufsz,
-                                   &bar[(k + 1) & 1], tmaps, WB_BATCH_USE_TMA, tid);
+                                   &bar[(k + 1) & 1], tmaps,
+                                   batch_tma_ok(Q, tmaps, bufs, bufsz), tid);
     cp_async_commit();
     const bool lim = Q.limiter == 1 && Q.lim_y && K >= 1;
     tile_compute<R, K, 1, TX, TY, POS ? WB_VAR_POSITIVITY : 0, CPT>(
@@ -178,7 +185,8 @@ __global__ void __launch_bounds__(TX * TY / CPT, batch_min_blocks(K, TX, TY))
       if (tid == LW) {
         cp_async_wait<1>();
         x = sW[s2].x;
-        if (WB_BATCH_USE_TMA && item_interior(sW[s2])) tensormap_acquire(tmaps + x);
+        if (batch_tma_ok(Q, tmaps, bufs, bufsz) && item_interior(sW[s2]))
+          tensormap_acquire(tmaps + x);
       }
       x = __shfl_sync(0xffffffffu, x, 0);
       args_copy_async(args + x, &sA[s2], tid - LW, 32);
@@ -186,7 +194,6 @@ __global__ void __launch_bounds__(TX * TY / CPT, batch_min_blocks(K, TX, TY))
     }
   }
   cp_async_wait<0>();
-#undef WB_BATCH_USE_TMA
 }
 
 // Start of a step, one thread per instance: the step's time step (stage_dt, whose FP64
