@@ -146,6 +146,7 @@ StageArgs<R> base_args(const wb_ctx *c) {
   A.kpoly = (R)g.kpoly;
   A.npoly = (R)(1.0 / (g.gamma - 1.0));
   A.lim_norm = (R)g.lim_norm;
+  A.lim_inorm = (R)(1.0 / g.lim_norm);
   A.lim_Mdx2 = (R)(g.lim_M * dx * dx);
   A.lim_Mdy2 = (R)(g.lim_M * dy * dy);
   A.lim_tol = (R)g.lim_tol;

@@ -365,8 +365,10 @@ __device__ __forceinline__ void limit_modes(const StageArgs<R> &A, const StageAr
     constexpr int NB = num_modes(K, BASIS);
     constexpr int M10 = mode_index(K, BASIS, 1, 0), M01 = mode_index(K, BASIS, 0, 1);
     R sx = base[M10 * mstride], sy = base[M01 * mstride];
-    R l1 = gminmod(A.lim_norm * sx, me - m0, m0 - mw, I.lim_Mdx2) / A.lim_norm;
-    R l2 = gminmod(A.lim_norm * sy, mn - m0, m0 - ms, I.lim_Mdy2) / A.lim_norm;
+    // minmod of the scaled slope and the mean differences, scaled back by 1 / norm (a
+    // product: a division per slope would cost a dozen instructions at every staged cell)
+    R l1 = gminmod(A.lim_norm * sx, me - m0, m0 - mw, I.lim_Mdx2) * A.lim_inorm;
+    R l2 = gminmod(A.lim_norm * sy, mn - m0, m0 - ms, I.lim_Mdy2) * A.lim_inorm;
     if (fabs(l1 - sx) > A.lim_tol || fabs(l2 - sy) > A.lim_tol) {
       base[M10 * mstride] = l1;
       base[M01 * mstride] = l2;

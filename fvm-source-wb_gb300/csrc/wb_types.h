@@ -96,6 +96,7 @@ struct alignas(16) StageArgs {
   R gx, gy;
   R rho0, p0, kpoly, npoly;   // npoly = 1/(gamma-1)
   R lim_norm, lim_Mdx2, lim_Mdy2, lim_tol;
+  R lim_inorm;                // 1 / lim_norm (the limited slope is scaled back by a product)
   R pos_eps;                  // positivity limiter floor (limiter 2)
   // separable equilibrium factors: x at volume points [nx*nq], x at faces [nx+1], y likewise
   const R *fxv, *fxf, *fyv, *fyf;
