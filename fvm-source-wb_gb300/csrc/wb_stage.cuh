@@ -747,15 +747,19 @@ __device__ __forceinline__ void tile_compute(const StageArgs<R> &A, const StageA
   // 2. limiter on every staged cell (means never change, so cells are independent)
   if (lim) {
     // neighbour means from the mode-0 planes (never written by the limiter) and, for the
-    // ring's first and last rows, from the staged second-ring rows
-    for (int e = tid; e < NV * RY * RXL; e += nthr) {
-      int rx = e % RXL, t1 = e / RXL, ry = t1 % RY, v = t1 / RY;
-      const R *mp = su + (v * NB) * RXY + ry * RX + rx;  // mode 0 of cell (ry, rx)
-      const R *sd = sm + v * 2 * RX + rx;
-      const R ms = ry > 0 ? mp[-RX] : sd[0];
-      const R mn = ry < RY - 1 ? mp[RX] : sd[RX];
-      limit_modes<R, K, BASIS>(A, I, su + (v * NB) * RXY + ry * RX + rx, RXY, mp[0], mp[-1], mp[1],
-                               ms, mn);
+    // ring's first and last rows, from the staged second-ring rows; a thread takes a cell
+    // and its four variables (the cell's index arithmetic once, not once per variable)
+    for (int e = tid; e < RY * RXL; e += nthr) {
+      const int rx = e % RXL, ry = e / RXL;
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        const R *mp = su + (v * NB) * RXY + ry * RX + rx;  // mode 0 of cell (ry, rx)
+        const R *sd = sm + v * 2 * RX + rx;
+        const R ms = ry > 0 ? mp[-RX] : sd[0];
+        const R mn = ry < RY - 1 ? mp[RX] : sd[RX];
+        limit_modes<R, K, BASIS>(A, I, su + (v * NB) * RXY + ry * RX + rx, RXY, mp[0], mp[-1],
+                                 mp[1], ms, mn);
+      }
     }
     __syncthreads();
   } else if (pos) {
