@@ -98,8 +98,10 @@ __device__ __forceinline__ bool batch_tma_ok(const StageArgs<R> &Q, const CUtens
 
 // Persistent batched stage for the items of one group (degree K, TX x TY tiles, CPT cells
 // per thread, one set of physical constants): CTAs stride over the group's work list; the
-// next item is staged (cp.async) while the current one is computed.  bufsz = the largest
-// tile buffer of the group.  One kernel per degree gives each its own register budget (and
+// next item is staged (one TMA copy through its instance's tensor map for an interior
+// tile, cp.async otherwise) while the current one is computed.  bufsz = the largest tile
+// buffer of the group; tmaps = the instances' tensor maps for this stage's input (or
+// null).  One kernel per degree gives each its own register budget (and
 // occupancy) and no runtime dispatch on K.  Q: the stage arguments of one instance of the
 // group, whose physical constants, boundary conditions, limiter and stage flags every
 // instance of the group shares; as a kernel parameter they are free operands of the
